@@ -1,0 +1,263 @@
+/*
+ * pyre_cuda.h — C ABI of the GB300 (sm_103a) wavefront path tracer.
+ *
+ * This is the drop-in boundary for the hot path of the Pyre renderer
+ * (Rust, crates/pyre). A host integration flattens Pyre's `Scene`, `Camera`
+ * and `PathIntegrator` into the plain descriptors below and calls
+ * `pyre_render` in place of the CLI's per-pixel closure loop
+ * (crates/pyre-cli/src/main.rs:253-286 driving Film::render,
+ * crates/pyre/src/film.rs:96-109).
+ *
+ * Conventions
+ *  - Every function returns an int status: PYRE_OK (0) or a negative
+ *    PYRE_ERR_* code; `pyre_last_error(ctx)` returns a message for the last
+ *    failure on that context (thread-local when ctx is NULL).
+ *  - The caller owns every host buffer it passes; the library copies what it
+ *    needs. Device buffers created by the library live behind the opaque
+ *    handles and are released by the matching destroy call.
+ *  - A context is used by one host thread at a time. Its work runs on the
+ *    context's own CUDA stream; every call returns after that work is done.
+ *  - Pointers tagged PYRE_MEM_DEVICE must be CUDA device pointers of the
+ *    context's device; PYRE_MEM_HOST pointers are ordinary host memory
+ *    (pinned or pageable).
+ */
+#ifndef PYRE_CUDA_H
+#define PYRE_CUDA_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PYRE_ABI_VERSION 1
+
+#define PYRE_OK 0
+#define PYRE_ERR_INVALID -1     /* bad argument or descriptor */
+#define PYRE_ERR_CUDA -2        /* CUDA runtime error (message has details) */
+#define PYRE_ERR_OOM -3         /* device or host allocation failed */
+#define PYRE_ERR_UNSUPPORTED -4 /* feature not available in this build */
+#define PYRE_ERR_OVERFLOW -5    /* a kernel detected a traversal-stack or queue overflow */
+#define PYRE_ERR_TIMEOUT -6     /* a bounded device-side wait ran out */
+
+#define PYRE_MEM_HOST 0
+#define PYRE_MEM_DEVICE 1
+
+typedef struct pyre_ctx pyre_ctx;
+typedef struct pyre_scene pyre_scene;
+
+/* ---------------------------------------------------------------- BVH --- */
+
+/* One node of the reference's binary BVH in its own layout
+ * (crates/pyre/src/geometry/bvh.rs:18-30, 32 bytes): DFS order, left child at
+ * index+1, `offset` = right child (interior) or first entry of the primitive
+ * index array (leaf), `n_primitives` = 0 for interior nodes. */
+typedef struct pyre_bvh2_node {
+    float bounds_min[3];
+    float bounds_max[3];
+    uint32_t offset;
+    uint16_t n_primitives;
+    uint8_t axis;
+    uint8_t pad;
+} pyre_bvh2_node;
+
+/* Builds the reference's SAH-binned BVH (12 bins, leaves of at most 8
+ * triangles; Bvh::build, crates/pyre/src/geometry/bvh.rs:45-64,180-409) over a
+ * triangle mesh. `nodes_out` must hold 2*n_triangles nodes and
+ * `prim_indices_out` n_triangles entries. Writes the node count. */
+int pyre_bvh_build(const float* positions, uint32_t n_vertices, const uint32_t* indices, uint32_t n_triangles,
+                   pyre_bvh2_node* nodes_out, uint32_t* prim_indices_out, uint32_t* n_nodes_out);
+
+/* -------------------------------------------------------------- Scene --- */
+
+/* TriangleMesh (crates/pyre/src/geometry/mesh.rs:5-11) plus, optionally, the
+ * BVH that MeshInstance::build made for it (Bvh::nodes() /
+ * Bvh::primitive_indices(), bvh.rs:66-72). When `bvh_nodes` is NULL the
+ * library builds the same BVH itself. */
+typedef struct pyre_mesh_desc {
+    const float* positions;      /* n_vertices * 3 */
+    uint32_t n_vertices;
+    const uint32_t* indices;     /* n_triangles * 3 */
+    uint32_t n_triangles;
+    const float* normals;        /* n_vertices * 3, or NULL (face normal fallback) */
+    const pyre_bvh2_node* bvh_nodes; /* or NULL */
+    uint32_t n_bvh_nodes;
+    const uint32_t* bvh_prim_indices; /* n_triangles, required with bvh_nodes */
+} pyre_mesh_desc;
+
+/* Primitive {instance, material_id} (crates/pyre/src/scene.rs:19-22) with the
+ * instance's optional translation-only motion (InstanceMotion, mesh.rs:46-60). */
+typedef struct pyre_instance_desc {
+    uint32_t mesh;
+    uint32_t material;
+    uint32_t has_motion;
+    float offset_t0[3];
+    float offset_t1[3];
+} pyre_instance_desc;
+
+#define PYRE_MAT_LAMBERTIAN 0 /* Lambertian{albedo=base_color}, material.rs:42-77 */
+#define PYRE_MAT_DISNEY 1     /* DisneyBsdf, material.rs:83-226 */
+
+typedef struct pyre_material_desc {
+    uint32_t kind;
+    float base_color[3];
+    float metallic;
+    float roughness;
+    float specular;
+} pyre_material_desc;
+
+/* DiffuseAreaQuadLight::new(p0, edge_u, edge_v, emission), light.rs:61-76 */
+typedef struct pyre_quad_light_desc {
+    float p0[3];
+    float edge_u[3];
+    float edge_v[3];
+    float emission[3];
+} pyre_quad_light_desc;
+
+/* HdriEnvironmentLight::new(width, height, pixels, intensity), light.rs:214-242 */
+typedef struct pyre_env_desc {
+    uint32_t width;
+    uint32_t height;
+    const float* rgb; /* width*height*3, row 0 = zenith */
+    float intensity;
+} pyre_env_desc;
+
+typedef struct pyre_scene_desc {
+    const pyre_mesh_desc* meshes;
+    uint32_t n_meshes;
+    const pyre_instance_desc* instances; /* scanned in this order = Scene::primitives */
+    uint32_t n_instances;
+    const pyre_material_desc* materials;
+    uint32_t n_materials;
+    const pyre_quad_light_desc* lights;
+    uint32_t n_lights;
+    const pyre_env_desc* env; /* or NULL */
+} pyre_scene_desc;
+
+/* ------------------------------------------------------------ Context --- */
+
+int pyre_version(void);
+int pyre_ctx_create(int device, pyre_ctx** out);
+int pyre_ctx_destroy(pyre_ctx* ctx);
+const char* pyre_last_error(const pyre_ctx* ctx);
+
+/* Uploads a flattened scene: collapses each mesh BVH into the device node
+ * layout, builds the top-level BVH over instance (swept) bounds and the HDRI
+ * sampling tables. */
+int pyre_scene_upload(pyre_ctx* ctx, const pyre_scene_desc* desc, pyre_scene** out);
+int pyre_scene_destroy(pyre_ctx* ctx, pyre_scene* scene);
+
+/* Sizes of an uploaded scene (Scene::triangle_count, scene.rs:154-159, plus
+ * the device layout). */
+typedef struct pyre_scene_info {
+    uint64_t n_triangles;
+    uint64_t n_nodes;        /* 64-byte device BVH nodes (all meshes + top level) */
+    uint64_t n_instances;    /* instances with geometry */
+    uint64_t triangle_bytes; /* device triangle records */
+    uint64_t node_bytes;
+    uint64_t device_bytes;   /* everything the scene holds on the device */
+} pyre_scene_info;
+int pyre_scene_get_info(const pyre_scene* scene, pyre_scene_info* out);
+
+/* --------------------------------------------------------- Intersect --- */
+
+/* Rays as the caller built them (directions are NOT normalized), like the
+ * shadow rays of Scene::occluded (scene.rs:102-140). `time` may be NULL (0). */
+typedef struct pyre_rays {
+    const float* origin;    /* n*3 */
+    const float* direction; /* n*3 */
+    const float* t_min;     /* n */
+    const float* t_max;     /* n */
+    const float* time;      /* n or NULL */
+} pyre_rays;
+
+/* Closest hit per ray: Scene::intersect (scene.rs:57-97) with the triangle id
+ * and barycentrics reported. kind: 0 miss, 1 surface, 2 quad light.
+ * instance = primitive index (or light index), triangle = index into the
+ * mesh's triangle list. Exact ties in t resolve to the lowest
+ * (instance, triangle). */
+typedef struct pyre_hits {
+    int32_t* kind;
+    int32_t* instance;
+    int32_t* triangle;
+    float* t;
+    float* u;
+    float* v;
+} pyre_hits;
+
+int pyre_intersect_closest(pyre_ctx* ctx, const pyre_scene* scene, const pyre_rays* rays, uint64_t n,
+                           pyre_hits* hits, int mem);
+/* Any hit against primitives only (Scene::occluded, scene.rs:120-140):
+ * occluded[i] = 1 when some triangle has t_min <= t < t_max. */
+int pyre_intersect_any(pyre_ctx* ctx, const pyre_scene* scene, const pyre_rays* rays, uint64_t n,
+                       uint8_t* occluded, int mem);
+
+/* ------------------------------------------------------------ Render --- */
+
+#define PYRE_CAMERA_PINHOLE 0   /* PinholeCamera::look_at, camera.rs:49-72 */
+#define PYRE_CAMERA_THIN_LENS 1 /* ThinLensCamera::look_at, camera.rs:105-122 */
+
+typedef struct pyre_camera_desc {
+    uint32_t kind;
+    float origin[3];
+    float target[3];
+    float up[3];
+    float vfov_deg;
+    float aspect;
+    float aperture_radius;
+    float focus_distance;
+} pyre_camera_desc;
+
+#define PYRE_ENV_ALIAS 0 /* 2D alias tables (default) */
+#define PYRE_ENV_CDF 1   /* the reference's inverse-CDF binary search */
+
+typedef struct pyre_render_params {
+    uint32_t width, height;          /* full image size (defines the ndc mapping) */
+    uint32_t spp_begin, spp_end;     /* samples s in [spp_begin, spp_end) per pixel */
+    uint32_t max_depth;              /* PathIntegrator::max_depth (8) */
+    uint32_t min_rr_depth;           /* PathIntegrator::min_rr_depth (3) */
+    uint32_t crop[4];                /* x0, y0, x1, y1; all zero = whole image */
+    uint32_t env_sampling;           /* PYRE_ENV_ALIAS or PYRE_ENV_CDF */
+    uint32_t wave_paths;             /* paths in flight per wave; 0 = automatic */
+    uint32_t block_size;             /* threads per block of the stage kernels; 0 = 256 */
+    uint32_t sort_by_material;       /* reorder the shade queue by material */
+    uint32_t use_graph;              /* capture one wave as a CUDA graph and replay it */
+    uint32_t reserved[4];
+} pyre_render_params;
+
+/* Film: per-pixel means over the sample range (PixelSample fields,
+ * integrator.rs:14-29), crop-sized, row-major, origin top-left. Any pointer
+ * may be NULL to skip that channel. */
+typedef struct pyre_film {
+    float* radiance; /* w*h*3 */
+    float* albedo;   /* w*h*3 */
+    float* normal;   /* w*h*3 */
+    float* depth;    /* w*h */
+    int mem;         /* PYRE_MEM_HOST or PYRE_MEM_DEVICE */
+} pyre_film;
+
+/* Statistics of the last render on the context. */
+typedef struct pyre_render_stats {
+    uint64_t samples;         /* paths started */
+    uint64_t extend_rays;     /* closest-hit rays traced */
+    uint64_t shadow_rays;     /* any-hit rays traced */
+    uint32_t waves;
+    uint32_t kernel_launches; /* stage-kernel launches (graph replays count their nodes) */
+    float ms_total;           /* device time of the render (CUDA events) */
+    float ms_extend, ms_shade, ms_shadow, ms_other; /* per-stage device time when profiling is on */
+} pyre_render_stats;
+
+/* Renders the sample range into `film`: the GPU equivalent of the CLI loop
+ * (main.rs:254-286) calling PathIntegrator::integrate (integrator.rs:57-232)
+ * once per (pixel, sample) with IndependentSampler(pixel_seed(x, y, s)). */
+int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                const pyre_render_params* params, pyre_film* film);
+int pyre_get_render_stats(const pyre_ctx* ctx, pyre_render_stats* out);
+/* Per-stage timing with CUDA events (adds synchronisation; off by default). */
+int pyre_set_stage_timing(pyre_ctx* ctx, int enabled);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYRE_CUDA_H */

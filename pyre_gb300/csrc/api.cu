@@ -1,0 +1,497 @@
+// api.cu — context, errors and scene upload of the C ABI.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <thread>
+
+#include "bvh_host.h"
+#include "internal.h"
+
+namespace pyre {
+
+static thread_local std::string g_tls_error;
+
+int set_error(pyre_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->error = msg;
+    else g_tls_error = msg;
+    return code;
+}
+
+int cuda_check(pyre_ctx* ctx, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return PYRE_OK;
+    std::string msg = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return set_error(ctx, e == cudaErrorMemoryAllocation ? PYRE_ERR_OOM : PYRE_ERR_CUDA, msg);
+}
+
+int ensure_workspace(pyre_ctx* ctx, Workspace& ws, size_t bytes) {
+    if (ws.bytes >= bytes) return PYRE_OK;
+    if (ws.ptr) {
+        cudaFree(ws.ptr);
+        ws.ptr = nullptr;
+        ws.bytes = 0;
+    }
+    // Any cached wave graph refers to the old buffers.
+    if (ctx->wave_graph) {
+        cudaGraphExecDestroy(ctx->wave_graph);
+        ctx->wave_graph = nullptr;
+        ctx->wave_graph_key.clear();
+    }
+    size_t rounded = (bytes + (1u << 20) - 1) & ~(size_t)((1u << 20) - 1);
+    cudaError_t e = cudaMalloc(&ws.ptr, rounded);
+    if (e != cudaSuccess) {
+        ws.ptr = nullptr;
+        return cuda_check(ctx, e, "cudaMalloc(workspace)");
+    }
+    ws.bytes = rounded;
+    return PYRE_OK;
+}
+
+int take_kernel_error(pyre_ctx* ctx) {
+    int flag = 0;
+    cudaError_t e = cudaMemcpyAsync(&flag, ctx->d_error, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "reading the kernel status");
+    if (flag != 0) {
+        cudaMemsetAsync(ctx->d_error, 0, sizeof(int), ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+        if (flag == PYRE_ERR_OVERFLOW)
+            return set_error(ctx, PYRE_ERR_OVERFLOW, "a kernel hit its traversal-stack or queue limit");
+        return set_error(ctx, flag, "a kernel reported an error status");
+    }
+    return PYRE_OK;
+}
+
+namespace {
+
+template <typename T>
+int upload(pyre_ctx* ctx, pyre_scene* sc, const std::vector<T>& host, T** out) {
+    *out = nullptr;
+    if (host.empty()) return PYRE_OK;
+    void* p = nullptr;
+    size_t bytes = host.size() * sizeof(T);
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(scene)");
+    sc->allocations.push_back(p);
+    sc->device_bytes += bytes;
+    e = cudaMemcpy(p, host.data(), bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMemcpy(scene)");
+    *out = (T*)p;
+    return PYRE_OK;
+}
+
+// Distribution1D (distribution.rs:40-61) in binary32: running sum of max(w,0),
+// normalised by the integral, uniform when the integral is not positive.
+float build_cdf(const float* w, uint32_t n, float* cdf) {
+    cdf[0] = 0.0f;
+    float acc = 0.0f;
+    for (uint32_t i = 0; i < n; ++i) {
+        acc += std::fmax(w[i], 0.0f);
+        cdf[i + 1] = acc;
+    }
+    if (acc > 0.0f) {
+        for (uint32_t i = 0; i <= n; ++i) cdf[i] /= acc;
+    } else {
+        for (uint32_t i = 0; i <= n; ++i) cdf[i] = (float)i / (float)n;
+    }
+    return acc;
+}
+
+// Vose's alias method over bin probabilities taken from the CDF differences.
+void build_alias(const float* cdf, uint32_t n, float2* table) {
+    std::vector<double> q(n);
+    double sum = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        q[i] = std::max(0.0, (double)cdf[i + 1] - (double)cdf[i]);
+        sum += q[i];
+    }
+    std::vector<uint32_t> small, large;
+    std::vector<double> scaled(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        scaled[i] = sum > 0.0 ? q[i] * (double)n / sum : 1.0;
+        (scaled[i] < 1.0 ? small : large).push_back(i);
+        table[i].x = 1.0f;
+        uint32_t self = i;
+        std::memcpy(&table[i].y, &self, 4);
+    }
+    while (!small.empty() && !large.empty()) {
+        uint32_t s = small.back(); small.pop_back();
+        uint32_t l = large.back(); large.pop_back();
+        table[s].x = (float)scaled[s];
+        std::memcpy(&table[s].y, &l, 4);
+        scaled[l] = (scaled[l] + scaled[s]) - 1.0;
+        (scaled[l] < 1.0 ? small : large).push_back(l);
+    }
+    for (uint32_t i : small) table[i].x = 1.0f;
+    for (uint32_t i : large) table[i].x = 1.0f;
+}
+
+}  // namespace
+}  // namespace pyre
+
+using namespace pyre;
+
+extern "C" {
+
+int pyre_version(void) { return PYRE_ABI_VERSION; }
+
+const char* pyre_last_error(const pyre_ctx* ctx) {
+    return ctx ? ctx->error.c_str() : g_tls_error.c_str();
+}
+
+int pyre_ctx_create(int device, pyre_ctx** out) {
+    if (!out) return set_error(nullptr, PYRE_ERR_INVALID, "pyre_ctx_create: out is NULL");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return cuda_check(nullptr, e, "cudaGetDeviceCount");
+    if (device < 0 || device >= count) return set_error(nullptr, PYRE_ERR_INVALID, "pyre_ctx_create: no such device");
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_check(nullptr, e, "cudaSetDevice");
+    pyre_ctx* ctx = new pyre_ctx();
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->d_error, sizeof(int))) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->d_counter, 64 * sizeof(unsigned int))) != cudaSuccess ||
+        (e = cudaMemset(ctx->d_error, 0, sizeof(int))) != cudaSuccess) {
+        int rc = cuda_check(nullptr, e, "pyre_ctx_create");
+        pyre_ctx_destroy(ctx);
+        return rc;
+    }
+    for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+    *out = ctx;
+    return PYRE_OK;
+}
+
+int pyre_ctx_destroy(pyre_ctx* ctx) {
+    if (!ctx) return PYRE_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->wave_graph) cudaGraphExecDestroy(ctx->wave_graph);
+    if (ctx->render_ws.ptr) cudaFree(ctx->render_ws.ptr);
+    if (ctx->io_ws.ptr) cudaFree(ctx->io_ws.ptr);
+    if (ctx->d_error) cudaFree(ctx->d_error);
+    if (ctx->d_counter) cudaFree(ctx->d_counter);
+    for (auto& ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return PYRE_OK;
+}
+
+int pyre_scene_destroy(pyre_ctx* ctx, pyre_scene* scene) {
+    if (!scene) return PYRE_OK;
+    if (ctx) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    for (void* p : scene->allocations) cudaFree(p);
+    delete scene;
+    return PYRE_OK;
+}
+
+int pyre_scene_upload(pyre_ctx* ctx, const pyre_scene_desc* desc, pyre_scene** out) {
+    if (!ctx || !desc || !out) return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_upload: NULL argument");
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    const uint32_t n_meshes = desc->n_meshes;
+    if (n_meshes && !desc->meshes) return set_error(ctx, PYRE_ERR_INVALID, "meshes is NULL");
+    if (desc->n_instances && !desc->instances) return set_error(ctx, PYRE_ERR_INVALID, "instances is NULL");
+    if (desc->n_materials && !desc->materials) return set_error(ctx, PYRE_ERR_INVALID, "materials is NULL");
+    if (desc->n_lights && !desc->lights) return set_error(ctx, PYRE_ERR_INVALID, "lights is NULL");
+
+    // ---- validate meshes and instances
+    for (uint32_t m = 0; m < n_meshes; ++m) {
+        const pyre_mesh_desc& md = desc->meshes[m];
+        if (md.n_triangles && (!md.positions || !md.indices))
+            return set_error(ctx, PYRE_ERR_INVALID, "mesh " + std::to_string(m) + ": positions/indices NULL");
+        for (uint64_t i = 0; i < 3ull * md.n_triangles; ++i)
+            if (md.indices[i] >= md.n_vertices)
+                return set_error(ctx, PYRE_ERR_INVALID, "mesh " + std::to_string(m) + ": vertex index out of range");
+        if (md.bvh_nodes) {
+            std::string why;
+            if (!validate_bvh2(md.bvh_nodes, md.n_bvh_nodes, md.bvh_prim_indices, md.n_triangles, &why))
+                return set_error(ctx, PYRE_ERR_INVALID, "mesh " + std::to_string(m) + ": " + why);
+        }
+    }
+    for (uint32_t i = 0; i < desc->n_instances; ++i) {
+        const pyre_instance_desc& id = desc->instances[i];
+        if (id.mesh >= n_meshes) return set_error(ctx, PYRE_ERR_INVALID, "instance mesh out of range");
+        if (id.material >= desc->n_materials)
+            return set_error(ctx, PYRE_ERR_INVALID, "instance material out of range");
+    }
+    for (uint32_t i = 0; i < desc->n_materials; ++i)
+        if (desc->materials[i].kind > PYRE_MAT_DISNEY) return set_error(ctx, PYRE_ERR_INVALID, "unknown material kind");
+    if (desc->env && (desc->env->width == 0 || desc->env->height == 0 || !desc->env->rgb))
+        return set_error(ctx, PYRE_ERR_INVALID, "environment map is empty");
+
+    // ---- per-mesh reference BVH2 (caller's, or built here in parallel)
+    std::vector<std::vector<pyre_bvh2_node>> built(n_meshes);
+    std::vector<std::vector<uint32_t>> built_prim(n_meshes);
+    {
+        std::atomic<uint32_t> next{0};
+        auto work = [&]() {
+            for (uint32_t m = next++; m < n_meshes; m = next++) {
+                const pyre_mesh_desc& md = desc->meshes[m];
+                if (md.bvh_nodes || md.n_triangles == 0) continue;
+                std::vector<Aabb> b;
+                std::vector<f3> c;
+                triangle_bounds(md.positions, md.indices, md.n_triangles, b, c);
+                build_bvh2(b, c, built[m], built_prim[m]);
+            }
+        };
+        unsigned nt = std::max(1u, std::min(std::thread::hardware_concurrency(), 32u));
+        nt = std::min<unsigned>(nt, std::max<uint32_t>(n_meshes, 1));
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
+    }
+
+    pyre_scene* sc = new pyre_scene();
+    static std::atomic<uint64_t> serial{1};
+    sc->serial = serial++;
+    auto fail = [&](int rc) { pyre_scene_destroy(ctx, sc); return rc; };
+
+    // ---- collapse BVHs, lay out triangle slots, index and normal buffers
+    std::vector<GpuNode> nodes;
+    std::vector<float4> tris;
+    std::vector<uint32_t> index;
+    std::vector<float> normal;
+    std::vector<int32_t> mesh_root(n_meshes, -1), mesh_index_base(n_meshes, 0), mesh_normal_base(n_meshes, -1);
+    std::vector<Aabb> mesh_box(n_meshes);
+    uint64_t total_tris = 0, total_verts_n = 0;
+    for (uint32_t m = 0; m < n_meshes; ++m) {
+        total_tris += desc->meshes[m].n_triangles;
+        if (desc->meshes[m].normals) total_verts_n += desc->meshes[m].n_vertices;
+    }
+    if (total_tris > (uint64_t)INT32_MAX / 3) return fail(set_error(ctx, PYRE_ERR_INVALID, "too many triangles"));
+    tris.reserve(3 * total_tris);
+    index.reserve(3 * total_tris);
+    normal.reserve(3 * total_verts_n);
+    for (uint32_t m = 0; m < n_meshes; ++m) {
+        const pyre_mesh_desc& md = desc->meshes[m];
+        mesh_index_base[m] = (int32_t)index.size();
+        if (md.n_triangles == 0) continue;
+        const pyre_bvh2_node* bn = md.bvh_nodes ? md.bvh_nodes : built[m].data();
+        uint32_t nn = md.bvh_nodes ? md.n_bvh_nodes : (uint32_t)built[m].size();
+        const uint32_t* prim = md.bvh_nodes ? md.bvh_prim_indices : built_prim[m].data();
+        int32_t slot_base = (int32_t)(tris.size() / 3);
+        mesh_root[m] = (int32_t)nodes.size();
+        mesh_box[m] = collapse_bvh2(bn, nn, (int32_t)nodes.size(), slot_base, nodes);
+        for (uint32_t k = 0; k < md.n_triangles; ++k) {
+            uint32_t t = prim[k];
+            const float* p0 = md.positions + 3 * (size_t)md.indices[3 * (size_t)t];
+            const float* p1 = md.positions + 3 * (size_t)md.indices[3 * (size_t)t + 1];
+            const float* p2 = md.positions + 3 * (size_t)md.indices[3 * (size_t)t + 2];
+            float id_bits;
+            std::memcpy(&id_bits, &t, 4);
+            tris.push_back(make_float4(p0[0], p0[1], p0[2], id_bits));
+            tris.push_back(make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.0f));
+            tris.push_back(make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.0f));
+        }
+        uint32_t vbase = md.normals ? (uint32_t)(normal.size() / 3) : 0;
+        if (md.normals) {
+            mesh_normal_base[m] = (int32_t)vbase;
+            normal.insert(normal.end(), md.normals, md.normals + 3 * (size_t)md.n_vertices);
+        }
+        for (uint64_t i = 0; i < 3ull * md.n_triangles; ++i) index.push_back(vbase + md.indices[i]);
+    }
+
+    // ---- instances and the top-level BVH over their swept bounds
+    std::vector<uint32_t> live;  // instances with geometry
+    std::vector<Aabb> ibox;
+    std::vector<f3> icent;
+    for (uint32_t i = 0; i < desc->n_instances; ++i) {
+        const pyre_instance_desc& id = desc->instances[i];
+        if (mesh_root[id.mesh] < 0) continue;
+        Aabb base = mesh_box[id.mesh];
+        Aabb w = base;
+        if (id.has_motion) {  // MeshInstance::world_bounds, mesh.rs:95-105
+            f3 o0 = mk3(id.offset_t0[0], id.offset_t0[1], id.offset_t0[2]);
+            f3 o1 = mk3(id.offset_t1[0], id.offset_t1[1], id.offset_t1[2]);
+            w.lo = vmin3(base.lo + o0, base.lo + o1);
+            w.hi = vmax3(base.hi + o0, base.hi + o1);
+        }
+        // The top level is an addition of this library: pad it so its test is
+        // never tighter than the reference's per-instance root test.
+        float mag = std::max({std::fabs(w.lo.x), std::fabs(w.lo.y), std::fabs(w.lo.z), std::fabs(w.hi.x),
+                              std::fabs(w.hi.y), std::fabs(w.hi.z), 1e-3f});
+        if (id.has_motion)
+            for (int k = 0; k < 3; ++k)
+                mag = std::max({mag, std::fabs(id.offset_t0[k]), std::fabs(id.offset_t1[k])});
+        float pad = mag * 1e-5f;
+        w.lo = w.lo - splat3(pad);
+        w.hi = w.hi + splat3(pad);
+        live.push_back(i);
+        ibox.push_back(w);
+        icent.push_back((w.lo + w.hi) * 0.5f);
+    }
+    std::vector<DevInstance> inst(live.size());
+    int32_t tlas_root = -1;
+    sc->slot_of_instance.assign(desc->n_instances, -1);
+    if (!live.empty()) {
+        std::vector<pyre_bvh2_node> tn;
+        std::vector<uint32_t> tp;
+        build_bvh2(ibox, icent, tn, tp);
+        tlas_root = (int32_t)nodes.size();
+        collapse_bvh2(tn.data(), (uint32_t)tn.size(), (int32_t)nodes.size(), 0, nodes);
+        for (size_t k = 0; k < tp.size(); ++k) {
+            uint32_t i = live[tp[k]];
+            const pyre_instance_desc& id = desc->instances[i];
+            DevInstance& I = inst[k];
+            std::memset(&I, 0, sizeof I);
+            const Aabb& rb = mesh_box[id.mesh];
+            I.lo[0] = rb.lo.x; I.lo[1] = rb.lo.y; I.lo[2] = rb.lo.z;
+            I.hi[0] = rb.hi.x; I.hi[1] = rb.hi.y; I.hi[2] = rb.hi.z;
+            I.blas_root = mesh_root[id.mesh];
+            I.has_motion = id.has_motion ? 1 : 0;
+            for (int c = 0; c < 3; ++c) { I.off0[c] = id.offset_t0[c]; I.off1[c] = id.offset_t1[c]; }
+            I.orig_id = (int32_t)i;
+            I.mesh = (int32_t)id.mesh;
+            I.material = id.material;
+            I.index_base = (uint32_t)mesh_index_base[id.mesh];
+            I.normal_base = mesh_normal_base[id.mesh];
+            I.tri_count = desc->meshes[id.mesh].n_triangles;
+            sc->slot_of_instance[i] = (int32_t)k;
+        }
+    }
+
+    // ---- materials and lights
+    std::vector<DevMaterial> mats(desc->n_materials);
+    for (uint32_t i = 0; i < desc->n_materials; ++i) {
+        const pyre_material_desc& m = desc->materials[i];
+        DevMaterial& d = mats[i];
+        for (int c = 0; c < 3; ++c) d.base[c] = m.base_color[c];
+        d.kind = m.kind; d.metallic = m.metallic; d.roughness = m.roughness; d.specular = m.specular; d.pad = 0;
+    }
+    std::vector<DevQuadLight> lights(desc->n_lights);
+    for (uint32_t i = 0; i < desc->n_lights; ++i) {  // DiffuseAreaQuadLight::new, light.rs:61-76
+        const pyre_quad_light_desc& l = desc->lights[i];
+        DevQuadLight& q = lights[i];
+        q.p0 = mk3(l.p0[0], l.p0[1], l.p0[2]);
+        q.edge_u = mk3(l.edge_u[0], l.edge_u[1], l.edge_u[2]);
+        q.edge_v = mk3(l.edge_v[0], l.edge_v[1], l.edge_v[2]);
+        q.emission = mk3(l.emission[0], l.emission[1], l.emission[2]);
+        q.crs = cross3(q.edge_u, q.edge_v);
+        q.area = len3(q.crs);
+        q.inv_cross_len_sq = 1.0f / len2(q.crs);
+        q.normal = normalize3(q.crs);
+    }
+
+    // ---- environment: texels, CDFs, per-bin pdfs, alias tables (light.rs:214-242)
+    std::vector<float4> env_px;
+    std::vector<float> marg_cdf, cond_cdf, marg_pdf, cond_pdf;
+    std::vector<float2> marg_alias, cond_alias;
+    DevEnv env{};
+    if (desc->env) {
+        const uint32_t w = desc->env->width, h = desc->env->height;
+        env_px.resize((size_t)w * h);
+        std::vector<float> weights((size_t)w * h);
+        for (uint32_t y = 0; y < h; ++y) {
+            float theta = ((float)y + 0.5f) / (float)h * 3.14159265358979323846f;
+            float sin_theta = std::fmax(std::sin(theta), 0.0f);
+            for (uint32_t x = 0; x < w; ++x) {
+                const float* p = desc->env->rgb + 3 * ((size_t)y * w + x);
+                env_px[(size_t)y * w + x] = make_float4(p[0], p[1], p[2], 0.0f);
+                float lum = 0.21267f * p[0] + 0.71516f * p[1] + 0.07217f * p[2];
+                weights[(size_t)y * w + x] = std::fmax(lum, 0.0f) * sin_theta;
+            }
+        }
+        cond_cdf.resize((size_t)h * (w + 1));
+        cond_pdf.resize((size_t)w * h);
+        cond_alias.resize((size_t)w * h);
+        std::vector<float> row_integral(h);
+        for (uint32_t y = 0; y < h; ++y) {
+            float* cdf = cond_cdf.data() + (size_t)y * (w + 1);
+            row_integral[y] = build_cdf(weights.data() + (size_t)y * w, w, cdf);
+            for (uint32_t x = 0; x < w; ++x) cond_pdf[(size_t)y * w + x] = (cdf[x + 1] - cdf[x]) * (float)w;
+            build_alias(cdf, w, cond_alias.data() + (size_t)y * w);
+        }
+        marg_cdf.resize(h + 1);
+        marg_pdf.resize(h);
+        marg_alias.resize(h);
+        build_cdf(row_integral.data(), h, marg_cdf.data());
+        for (uint32_t y = 0; y < h; ++y) marg_pdf[y] = (marg_cdf[y + 1] - marg_cdf[y]) * (float)h;
+        build_alias(marg_cdf.data(), h, marg_alias.data());
+        env.width = w;
+        env.height = h;
+        env.intensity = desc->env->intensity;
+    }
+
+    // ---- upload
+    DevScene& D = sc->dev;
+    std::memset(&D, 0, sizeof D);
+    int rc;
+    GpuNode* d_nodes = nullptr;
+    if ((rc = upload(ctx, sc, nodes, &d_nodes)) != PYRE_OK) return fail(rc);
+    D.nodes = reinterpret_cast<const float4*>(d_nodes);
+    float4* d_tris = nullptr;
+    if ((rc = upload(ctx, sc, tris, &d_tris)) != PYRE_OK) return fail(rc);
+    D.tris = d_tris;
+    DevInstance* d_inst = nullptr;
+    if ((rc = upload(ctx, sc, inst, &d_inst)) != PYRE_OK) return fail(rc);
+    D.inst = d_inst;
+    D.n_inst = (uint32_t)inst.size();
+    D.tlas_root = tlas_root;
+    uint32_t* d_index = nullptr;
+    if ((rc = upload(ctx, sc, index, &d_index)) != PYRE_OK) return fail(rc);
+    D.index = d_index;
+    float* d_normal = nullptr;
+    if ((rc = upload(ctx, sc, normal, &d_normal)) != PYRE_OK) return fail(rc);
+    D.normal = d_normal;
+    DevMaterial* d_mats = nullptr;
+    if ((rc = upload(ctx, sc, mats, &d_mats)) != PYRE_OK) return fail(rc);
+    D.materials = d_mats;
+    D.n_materials = (uint32_t)mats.size();
+    DevQuadLight* d_lights = nullptr;
+    if ((rc = upload(ctx, sc, lights, &d_lights)) != PYRE_OK) return fail(rc);
+    D.lights = d_lights;
+    D.n_lights = (uint32_t)lights.size();
+    if (desc->env) {
+        float4* px = nullptr;
+        float *mc = nullptr, *cc = nullptr, *mp = nullptr, *cp = nullptr;
+        float2 *ma = nullptr, *ca = nullptr;
+        if ((rc = upload(ctx, sc, env_px, &px)) != PYRE_OK || (rc = upload(ctx, sc, marg_cdf, &mc)) != PYRE_OK ||
+            (rc = upload(ctx, sc, cond_cdf, &cc)) != PYRE_OK || (rc = upload(ctx, sc, marg_pdf, &mp)) != PYRE_OK ||
+            (rc = upload(ctx, sc, cond_pdf, &cp)) != PYRE_OK || (rc = upload(ctx, sc, marg_alias, &ma)) != PYRE_OK ||
+            (rc = upload(ctx, sc, cond_alias, &ca)) != PYRE_OK)
+            return fail(rc);
+        env.pixels = px; env.marg_cdf = mc; env.cond_cdf = cc; env.marg_pdf = mp; env.cond_pdf = cp;
+        env.marg_alias = ma; env.cond_alias = ca;
+        D.has_env = 1;
+        D.env = env;
+    }
+    D.error_flag = ctx->d_error;
+    sc->n_triangles = (uint32_t)total_tris;
+    sc->n_nodes = nodes.size();
+    *out = sc;
+    return PYRE_OK;
+}
+
+int pyre_scene_get_info(const pyre_scene* scene, pyre_scene_info* out) {
+    if (!scene || !out) return PYRE_ERR_INVALID;
+    out->n_triangles = scene->n_triangles;
+    out->n_nodes = scene->n_nodes;
+    out->n_instances = scene->dev.n_inst;
+    out->triangle_bytes = (uint64_t)scene->n_triangles * 48;
+    out->node_bytes = scene->n_nodes * 64;
+    out->device_bytes = scene->device_bytes;
+    return PYRE_OK;
+}
+
+int pyre_get_render_stats(const pyre_ctx* ctx, pyre_render_stats* out) {
+    if (!ctx || !out) return PYRE_ERR_INVALID;
+    *out = ctx->stats;
+    return PYRE_OK;
+}
+
+int pyre_set_stage_timing(pyre_ctx* ctx, int enabled) {
+    if (!ctx) return PYRE_ERR_INVALID;
+    ctx->stage_timing = enabled ? 1 : 0;
+    return PYRE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,56 @@
+// bvh_host.h — host-side BVH construction and the device node layout.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "pyre_math.cuh"
+#include "../../include/pyre_cuda.h"
+
+namespace pyre {
+
+struct Aabb {
+    f3 lo, hi;
+};
+
+// Device BVH node: the two children of one binary node, 64 bytes, one cache
+// line per visit. Children's boxes are stored in the parent so a visit tests
+// both boxes with the node's four 16-byte loads.
+//   a = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   b = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   c = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   d = (child0, child1, count0, count1)
+// child with count > 0: leaf, child = first triangle (or instance) slot;
+// count == 0 and child >= 0: interior node index; child < 0: empty slot.
+struct alignas(16) GpuNode {
+    float a[4];
+    float b[4];
+    float c[4];
+    int32_t d[4];
+};
+static_assert(sizeof(GpuNode) == 64, "GpuNode is one 64-byte line");
+
+// Builds the reference's binned-SAH binary BVH (bvh.rs:45-64,180-409) over
+// arbitrary primitive bounds/centroids. Output uses the reference node layout
+// (pyre_bvh2_node): DFS pre-order, left child = index + 1.
+void build_bvh2(const std::vector<Aabb>& prim_bounds, const std::vector<f3>& prim_centroids,
+                std::vector<pyre_bvh2_node>& nodes, std::vector<uint32_t>& prim_indices);
+
+// Per-triangle bounds and centroids as MeshInstance::build computes them
+// (mesh.rs:77-87, triangle_bounds / triangle_centroid mesh.rs:32-40).
+void triangle_bounds(const float* positions, const uint32_t* indices, uint32_t n_triangles,
+                     std::vector<Aabb>& bounds, std::vector<f3>& centroids);
+
+// Checks that a caller-supplied reference BVH is well formed (indices in
+// range, every primitive referenced once). Returns false with a message.
+bool validate_bvh2(const pyre_bvh2_node* nodes, uint32_t n_nodes, const uint32_t* prim, uint32_t n_prims,
+                   std::string* why);
+
+// Collapses a reference binary BVH into device nodes. `node_base` is the
+// global index of the first emitted node, `slot_base` the global index of the
+// first triangle/instance slot (leaf offsets are added to it). Returns the
+// root's box. A root that is itself a leaf becomes one device node with an
+// empty second child.
+Aabb collapse_bvh2(const pyre_bvh2_node* nodes, uint32_t n_nodes, int32_t node_base, int32_t slot_base,
+                   std::vector<GpuNode>& out);
+
+}  // namespace pyre

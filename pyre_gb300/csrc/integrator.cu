@@ -1,0 +1,789 @@
+// integrator.cu — wavefront path tracer and ray-query kernels for sm_103a.
+//
+// One render = waves of paths. A wave holds K samples of every pixel of the
+// crop (path i -> sample s_base + i / npix, pixel i % npix), so the film can
+// sum sample radiance in the same order as the CLI loop
+// (crates/pyre-cli/src/main.rs:260-285). Each wave runs
+//   raygen -> [extend -> shade -> shadow] x max_depth -> accumulate
+// over structure-of-arrays path state in HBM, with the live paths and the
+// shadow rays kept in compacted queues (warp-aggregated appends). Every path
+// carries its own Xoshiro256++ state, so the sampler draws happen in the
+// reference's order: jitter x/y, lens x/y, time at raygen; then per surface
+// vertex one vec2 per quad light, one vec2 for the environment, one vec2 for
+// the BSDF sample and one f32 for Russian roulette (integrator.rs:307-375).
+// NEE contributions are computed at shade time assuming visibility and parked
+// in per-path slots; the shadow stage clears the slot of an occluded ray; the
+// next shade (or the accumulate stage) adds the surviving slots in light
+// order, which is the reference's summation order.
+#include <cooperative_groups.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "internal.h"
+#include "shading.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace pyre {
+
+#define PYRE_MAX_DEPTH 64
+
+struct WaveCtl {
+    uint32_t wave;
+    uint32_t s_base;
+    uint32_t k_valid;
+    uint32_t n_valid;
+    uint32_t count[PYRE_MAX_DEPTH + 1];   // extend queue sizes per depth
+    uint32_t scount[PYRE_MAX_DEPTH];      // shadow queue sizes per depth
+    uint32_t fetch[2 * PYRE_MAX_DEPTH];   // work counters of extend / shadow
+    unsigned long long extend_rays, shadow_rays, samples;
+};
+
+struct WaveParams {
+    DevCamera cam;
+    uint32_t width, height;
+    uint32_t cx0, cy0, cw, ch, npix;
+    uint32_t spp_begin, spp_end, k_per_wave;
+    uint32_t max_depth, min_rr;
+    uint32_t ns;  // NEE slots per path: lights (+1 for the environment)
+    int env_cdf;
+};
+
+struct PathSoA {
+    float4* ray_o;     // origin.xyz
+    float4* ray_d;     // direction.xyz, time
+    float4* hit;       // t, u, v, triangle slot (bits)
+    int32_t* hit_inst; // instance slot; -1 miss; -2-l quad light l
+    uint4* rng;        // 2 per path
+    float4* beta;      // throughput.xyz, pdf of the last BSDF sample
+    float4* L;         // radiance.xyz
+    float4* aov_a;     // albedo.xyz, depth
+    float4* aov_n;     // normal.xyz
+    float4* pend;      // ns per path: NEE contribution.xyz, w = 1 while pending
+    float4* sh_o;      // ns per path: shadow origin.xyz, t_max
+    float4* sh_d;      // ns per path: shadow direction.xyz, time
+    uint32_t* q[2];
+    uint32_t* sq;
+    float4* acc_r;     // per crop pixel: radiance sum.xyz, depth sum
+    float4* acc_a;     // albedo sum
+    float4* acc_n;     // normal sum
+    WaveCtl* ctl;
+};
+
+__device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(counter, g.size());
+    base = g.shfl(base, 0);
+    return base + g.thread_rank();
+}
+
+__device__ __forceinline__ void store_rng(uint4* r, uint32_t i, const Rng& g) {
+    r[2 * (size_t)i] = make_uint4((uint32_t)g.s0, (uint32_t)(g.s0 >> 32), (uint32_t)g.s1, (uint32_t)(g.s1 >> 32));
+    r[2 * (size_t)i + 1] = make_uint4((uint32_t)g.s2, (uint32_t)(g.s2 >> 32), (uint32_t)g.s3, (uint32_t)(g.s3 >> 32));
+}
+__device__ __forceinline__ Rng load_rng(const uint4* r, uint32_t i) {
+    uint4 a = r[2 * (size_t)i], b = r[2 * (size_t)i + 1];
+    Rng g;
+    g.s0 = (uint64_t)a.x | ((uint64_t)a.y << 32);
+    g.s1 = (uint64_t)a.z | ((uint64_t)a.w << 32);
+    g.s2 = (uint64_t)b.x | ((uint64_t)b.y << 32);
+    g.s3 = (uint64_t)b.z | ((uint64_t)b.w << 32);
+    return g;
+}
+
+// ------------------------------------------------------------------ wave --
+__global__ void k_wave_begin(WaveCtl* ctl, uint32_t spp_begin, uint32_t spp_end, uint32_t K, uint32_t npix) {
+    if (threadIdx.x != 0) return;
+    uint32_t s_base = spp_begin + ctl->wave * K;
+    uint32_t k_valid = s_base < spp_end ? min(K, spp_end - s_base) : 0u;
+    ctl->s_base = s_base;
+    ctl->k_valid = k_valid;
+    ctl->n_valid = k_valid * npix;
+    for (int d = 0; d <= PYRE_MAX_DEPTH; ++d) ctl->count[d] = 0;
+    for (int d = 0; d < PYRE_MAX_DEPTH; ++d) ctl->scount[d] = 0;
+    for (int d = 0; d < 2 * PYRE_MAX_DEPTH; ++d) ctl->fetch[d] = 0;
+    ctl->count[0] = k_valid * npix;
+}
+
+__global__ void k_wave_end(WaveCtl* ctl, uint32_t max_depth) {
+    if (threadIdx.x != 0) return;
+    unsigned long long e = 0, s = 0;
+    for (uint32_t d = 0; d < max_depth; ++d) { e += ctl->count[d]; s += ctl->scount[d]; }
+    ctl->extend_rays += e;
+    ctl->shadow_rays += s;
+    ctl->samples += ctl->n_valid;
+    ctl->wave += 1;
+}
+
+// main.rs:261-273: seed, jitter, ndc, lens, time, Camera::generate_ray.
+__global__ void k_raygen(PathSoA P, WaveParams W) {
+    const uint32_t n = P.ctl->n_valid;
+    const uint32_t s_base = P.ctl->s_base;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t k = i / W.npix, p = i - k * W.npix;
+        uint32_t x = W.cx0 + p % W.cw, y = W.cy0 + p / W.cw;
+        Rng g;
+        g.seed(pixel_seed(x, y, s_base + k));
+        float jx = g.next_f32(), jy = g.next_f32();
+        f2 ndc;
+        ndc.x = 2.0f * ((float)x + jx) / (float)W.width - 1.0f;
+        ndc.y = 1.0f - 2.0f * ((float)y + jy) / (float)W.height;
+        f2 lens = g.next_vec2();
+        float time = g.next_f32();
+        f3 o, d;
+        camera_ray(W.cam, ndc, lens, &o, &d);
+        P.ray_o[i] = make_float4(o.x, o.y, o.z, 1e-4f);
+        P.ray_d[i] = make_float4(d.x, d.y, d.z, time);
+        store_rng(P.rng, i, g);
+        P.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        P.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        P.aov_a[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        P.aov_n[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (uint32_t s = 0; s < W.ns; ++s) P.pend[(size_t)i * W.ns + s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+// ---------------------------------------------------------------- extend --
+__global__ void __launch_bounds__(128) k_extend(DevScene S, PathSoA P, uint32_t depth) {
+    const uint32_t n = P.ctl->count[depth];
+    const uint32_t* qin = P.q[depth & 1];
+    uint32_t* fetch = &P.ctl->fetch[2 * depth];
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(fetch, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        uint32_t j = base + lane;
+        if (j < n) {
+            uint32_t i = depth == 0 ? j : qin[j];
+            float4 ro = P.ray_o[i], rd = P.ray_d[i];
+            TraceRay r;
+            r.o = mk3(ro.x, ro.y, ro.z);
+            r.d = mk3(rd.x, rd.y, rd.z);
+            r.tmin = 1e-4f;
+            r.tmax = __int_as_float(0x7f800000);
+            r.time = rd.w;
+            TraceHit h;
+            trace_closest_with_lights(S, r, &h);
+            int32_t code = h.light >= 0 ? -2 - h.light : h.inst;
+            P.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+            P.hit_inst[i] = code;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- shadow --
+__global__ void __launch_bounds__(128) k_shadow(DevScene S, PathSoA P, uint32_t depth) {
+    const uint32_t n = P.ctl->scount[depth];
+    uint32_t* fetch = &P.ctl->fetch[2 * depth + 1];
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(fetch, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        uint32_t j = base + lane;
+        if (j < n) {
+            uint32_t target = P.sq[j];
+            float4 so = P.sh_o[target], sd = P.sh_d[target];
+            TraceRay r;
+            r.o = mk3(so.x, so.y, so.z);
+            r.d = mk3(sd.x, sd.y, sd.z);
+            r.tmin = 1e-3f;
+            r.tmax = so.w;
+            r.time = sd.w;
+            TraceHit h;
+            if (trace_scene<true>(S, r, &h)) P.pend[target] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
+// ----------------------------------------------------------------- shade --
+// One path vertex of PathIntegrator::integrate (integrator.rs:242-388).
+__global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+    const uint32_t n = P.ctl->count[depth];
+    const uint32_t* qin = P.q[depth & 1];
+    uint32_t* qout = P.q[(depth + 1) & 1];
+    uint32_t* next_count = &P.ctl->count[depth + 1];
+    uint32_t* shadow_count = &P.ctl->scount[depth];
+    const bool last_was_specular = depth == 0;  // no specular BSDFs: only camera rays
+    const float INF = __int_as_float(0x7f800000);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t i = depth == 0 ? j : qin[j];
+        float4 Lq = P.L[i];
+        f3 L = mk3(Lq.x, Lq.y, Lq.z);
+        // Contributions left by the previous vertex's NEE, in light order.
+        if (depth > 0) {
+            for (uint32_t s = 0; s < W.ns; ++s) {
+                float4 c = P.pend[(size_t)i * W.ns + s];
+                if (c.w != 0.0f) {
+                    L = L + mk3(c.x, c.y, c.z);
+                    P.pend[(size_t)i * W.ns + s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                }
+            }
+        }
+        const float4 bq = P.beta[i];
+        f3 beta = mk3(bq.x, bq.y, bq.z);
+        const float last_pdf = bq.w;
+        const float4 ro = P.ray_o[i], rd = P.ray_d[i];
+        const f3 ray_o = mk3(ro.x, ro.y, ro.z), ray_d = mk3(rd.x, rd.y, rd.z);
+        const float time = rd.w;
+        const float4 hq = P.hit[i];
+        const int32_t code = P.hit_inst[i];
+        bool alive = false;
+
+        if (code == -1) {
+            // Escaped: environment radiance with MIS against the BSDF arm (integrator.rs:243-259).
+            if (S.has_env) {
+                f3 le = env_le(S.env, ray_d);
+                if (!is_zero3(le)) {
+                    if (last_was_specular) L = L + beta * le;
+                    else {
+                        float pdf_env = env_pdf(S.env, ray_d);
+                        float w = power_heuristic(last_pdf, pdf_env);
+                        L = L + beta * le * w;
+                    }
+                }
+            }
+        } else if (code <= -2) {
+            // Quad light hit (integrator.rs:262-295).
+            const DevQuadLight& Lt = S.lights[-2 - code];
+            if (depth == 0) {
+                P.aov_a[i] = make_float4(1.0f, 1.0f, 1.0f, hq.x);
+                P.aov_n[i] = make_float4(Lt.normal.x, Lt.normal.y, Lt.normal.z, 0.0f);
+            }
+            f3 le = dot3(Lt.normal, -ray_d) > 0.0f ? Lt.emission : splat3(0.0f);
+            if (last_was_specular) L = L + beta * le;
+            else {
+                float pdf_light = quad_pdf(Lt, ray_o, ray_d);
+                float w = power_heuristic(last_pdf, pdf_light);
+                L = L + beta * le * w;
+            }
+        } else {
+            // Surface hit: position and shading normal (mesh.rs:126-136,147).
+            const DevInstance& I = S.inst[code];
+            const float t = hq.x, u = hq.y, v = hq.z;
+            const int32_t slot = __float_as_int(hq.w);
+            f3 off = splat3(0.0f);
+            if (I.has_motion) off = motion_offset(I, time);
+            const bool moved = !is_zero3(off);
+            f3 o_local = moved ? ray_o - off : ray_o;
+            f3 p = o_local + ray_d * t;
+            if (moved) p = p + off;
+            const float4 A = __ldg(S.tris + 3 * (size_t)slot);
+            f3 ns;
+            if (I.normal_base >= 0) {
+                const uint32_t tri = __float_as_uint(A.w);
+                const uint32_t* ix = S.index + I.index_base + 3 * (size_t)tri;
+                const uint32_t a = ix[0], b = ix[1], c = ix[2];
+                const f3 na = mk3(S.normal[3 * (size_t)a], S.normal[3 * (size_t)a + 1], S.normal[3 * (size_t)a + 2]);
+                const f3 nb = mk3(S.normal[3 * (size_t)b], S.normal[3 * (size_t)b + 1], S.normal[3 * (size_t)b + 2]);
+                const f3 nc = mk3(S.normal[3 * (size_t)c], S.normal[3 * (size_t)c + 1], S.normal[3 * (size_t)c + 2]);
+                const float w = 1.0f - u - v;
+                ns = normalize3(w * na + u * nb + v * nc);
+            } else {
+                const float4 B = __ldg(S.tris + 3 * (size_t)slot + 1), C = __ldg(S.tris + 3 * (size_t)slot + 2);
+                ns = normalize3(cross3(mk3(B.x, B.y, B.z), mk3(C.x, C.y, C.z)));
+            }
+            const Bsdf mat = load_bsdf(S, I.material);
+            if (depth == 0) {
+                P.aov_a[i] = make_float4(mat.base.x, mat.base.y, mat.base.z, t);
+                P.aov_n[i] = make_float4(ns.x, ns.y, ns.z, 0.0f);
+            }
+            const Frame3 fr = frame_from_normal(ns);
+            const f3 wo = to_local(fr, -ray_d);
+            if (wo.z > 0.0f) {
+                Rng g = load_rng(P.rng, i);
+                const f3 p_off = p + 1e-3f * ns;
+                // NEE over every quad light (integrator.rs:307-333).
+                for (uint32_t l = 0; l < S.n_lights; ++l) {
+                    f2 ul = g.next_vec2();
+                    const DevQuadLight& Lt = S.lights[l];
+                    f3 lpos, lwi;
+                    float lpdf;
+                    if (!quad_sample(Lt, p, ul, &lpos, &lwi, &lpdf)) continue;
+                    if (lpdf <= 0.0f || is_zero3(Lt.emission)) continue;
+                    f3 wi = to_local(fr, lwi);
+                    if (wi.z <= 0.0f) continue;
+                    f3 f = bsdf_eval(mat, wo, wi);
+                    if (is_zero3(f)) continue;
+                    f3 target = lpos - 1e-3f * lwi;
+                    // Scene::occluded (scene.rs:120-140)
+                    f3 tf = target - p_off;
+                    float dist = len3(tf);
+                    float pdf_b = bsdf_pdf(mat, wo, wi);
+                    float w = power_heuristic(lpdf, pdf_b);
+                    f3 contrib = beta * f * Lt.emission * wi.z * w / lpdf;
+                    size_t sidx = (size_t)i * W.ns + l;
+                    P.pend[sidx] = make_float4(contrib.x, contrib.y, contrib.z, 1.0f);
+                    if (dist > 0.0f) {
+                        f3 dir = tf / dist;
+                        P.sh_o[sidx] = make_float4(p_off.x, p_off.y, p_off.z, dist - 1e-3f);
+                        P.sh_d[sidx] = make_float4(dir.x, dir.y, dir.z, time);
+                        P.sq[append_slot(shadow_count)] = (uint32_t)sidx;
+                    }
+                }
+                // Environment NEE arm (integrator.rs:335-354).
+                if (S.has_env) {
+                    f2 ue = g.next_vec2();
+                    f3 ewi, eli;
+                    float epdf;
+                    env_sample(S.env, ue, W.env_cdf, &ewi, &eli, &epdf);
+                    if (epdf > 0.0f && !is_zero3(eli)) {
+                        f3 wi = to_local(fr, ewi);
+                        if (wi.z > 0.0f) {
+                            f3 f = bsdf_eval(mat, wo, wi);
+                            if (!is_zero3(f)) {
+                                float pdf_b = bsdf_pdf(mat, wo, wi);
+                                float w = power_heuristic(epdf, pdf_b);
+                                f3 contrib = beta * f * eli * wi.z * w / epdf;
+                                size_t sidx = (size_t)i * W.ns + S.n_lights;
+                                P.pend[sidx] = make_float4(contrib.x, contrib.y, contrib.z, 1.0f);
+                                P.sh_o[sidx] = make_float4(p_off.x, p_off.y, p_off.z, INF);
+                                P.sh_d[sidx] = make_float4(ewi.x, ewi.y, ewi.z, time);
+                                P.sq[append_slot(shadow_count)] = (uint32_t)sidx;
+                            }
+                        }
+                    }
+                }
+                // BSDF sample, throughput, Russian roulette (integrator.rs:356-375).
+                f3 bwi, bf;
+                float bpdf;
+                if (bsdf_sample(mat, wo, g.next_vec2(), &bwi, &bf, &bpdf) && bpdf > 0.0f) {
+                    float cos_wi = fabsf(bwi.z);
+                    if (cos_wi != 0.0f) {
+                        beta = beta * (bf * cos_wi / bpdf);
+                        bool survive = true;
+                        if (depth >= W.min_rr) {
+                            float q = clampf_(1.0f - max_elem3(beta), 0.05f, 0.95f);
+                            if (g.next_f32() < q) survive = false;
+                            else beta = beta / (1.0f - q);
+                        }
+                        if (survive) {
+                            // Next ray (integrator.rs:377-387).
+                            f3 nd = to_world(fr, bwi);
+                            P.ray_o[i] = make_float4(p_off.x, p_off.y, p_off.z, 1e-4f);
+                            P.ray_d[i] = make_float4(nd.x, nd.y, nd.z, time);
+                            P.beta[i] = make_float4(beta.x, beta.y, beta.z, bpdf);
+                            alive = true;
+                        }
+                    }
+                }
+                store_rng(P.rng, i, g);
+            }
+        }
+        P.L[i] = make_float4(L.x, L.y, L.z, 0.0f);
+        if (alive && depth + 1 < W.max_depth) qout[append_slot(next_count)] = i;
+    }
+}
+
+// ------------------------------------------------------------ accumulate --
+// Film sums in sample order (main.rs:275-278): pending NEE of the last vertex
+// is added to the path radiance first.
+__global__ void k_accumulate(PathSoA P, WaveParams W) {
+    const uint32_t kv = P.ctl->k_valid;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W.npix; p += gridDim.x * blockDim.x) {
+        float4 ar = P.acc_r[p], aa = P.acc_a[p], an = P.acc_n[p];
+        for (uint32_t k = 0; k < kv; ++k) {
+            uint32_t i = k * W.npix + p;
+            float4 Lq = P.L[i];
+            f3 L = mk3(Lq.x, Lq.y, Lq.z);
+            for (uint32_t s = 0; s < W.ns; ++s) {
+                float4 c = P.pend[(size_t)i * W.ns + s];
+                if (c.w != 0.0f) L = L + mk3(c.x, c.y, c.z);
+            }
+            float4 a = P.aov_a[i], nn = P.aov_n[i];
+            ar.x += L.x; ar.y += L.y; ar.z += L.z; ar.w += a.w;
+            aa.x += a.x; aa.y += a.y; aa.z += a.z;
+            an.x += nn.x; an.y += nn.y; an.z += nn.z;
+        }
+        P.acc_r[p] = ar; P.acc_a[p] = aa; P.acc_n[p] = an;
+    }
+}
+
+// Mean over the sample range (main.rs:280-285).
+__global__ void k_finalize(PathSoA P, uint32_t npix, float inv_spp, float* rad, float* alb, float* nor, float* dep) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        float4 ar = P.acc_r[p], aa = P.acc_a[p], an = P.acc_n[p];
+        if (rad) { rad[3 * (size_t)p] = ar.x * inv_spp; rad[3 * (size_t)p + 1] = ar.y * inv_spp; rad[3 * (size_t)p + 2] = ar.z * inv_spp; }
+        if (alb) { alb[3 * (size_t)p] = aa.x * inv_spp; alb[3 * (size_t)p + 1] = aa.y * inv_spp; alb[3 * (size_t)p + 2] = aa.z * inv_spp; }
+        if (nor) { nor[3 * (size_t)p] = an.x * inv_spp; nor[3 * (size_t)p + 1] = an.y * inv_spp; nor[3 * (size_t)p + 2] = an.z * inv_spp; }
+        if (dep) dep[p] = ar.w * inv_spp;
+    }
+}
+
+// ------------------------------------------------------ ray-query kernels --
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_intersect(DevScene S, const float* __restrict__ org, const float* __restrict__ dir,
+                                                   const float* __restrict__ tmin, const float* __restrict__ tmax,
+                                                   const float* __restrict__ time, uint32_t n, unsigned int* counter,
+                                                   int32_t* kind, int32_t* inst, int32_t* tri, float* tt, float* uu,
+                                                   float* vv, uint8_t* occluded) {
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(counter, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        uint32_t i = base + lane;
+        if (i >= n) continue;
+        TraceRay r;
+        r.o = mk3(org[3 * (size_t)i], org[3 * (size_t)i + 1], org[3 * (size_t)i + 2]);
+        r.d = mk3(dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]);
+        r.tmin = tmin[i];
+        r.tmax = tmax[i];
+        r.time = time ? time[i] : 0.0f;
+        TraceHit h;
+        if (ANY) {
+            occluded[i] = trace_scene<true>(S, r, &h) ? 1 : 0;
+        } else {
+            trace_closest_with_lights(S, r, &h);
+            if (h.light >= 0) {
+                kind[i] = 2; inst[i] = h.light; tri[i] = -1;
+                tt[i] = h.t; uu[i] = 0.0f; vv[i] = 0.0f;
+            } else if (h.inst >= 0) {
+                kind[i] = 1;
+                inst[i] = S.inst[h.inst].orig_id;
+                tri[i] = (int32_t)__float_as_uint(__ldg(S.tris + 3 * (size_t)h.tri).w);
+                tt[i] = h.t; uu[i] = h.u; vv[i] = h.v;
+            } else {
+                kind[i] = 0; inst[i] = -1; tri[i] = -1;
+                tt[i] = __int_as_float(0x7f800000); uu[i] = 0.0f; vv[i] = 0.0f;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------ host side --
+namespace {
+
+template <typename K>
+int grid_for(pyre_ctx* ctx, K kernel, int block, size_t smem = 0) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+    return std::max(1, per_sm) * std::max(1, ctx->num_sms);
+}
+
+// Carves the workspace into typed arrays (256-byte aligned).
+struct Carver {
+    char* base;
+    size_t off = 0;
+    template <typename T>
+    T* take(size_t count) {
+        off = (off + 255) & ~(size_t)255;
+        T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* out) {
+    Carver c{base};
+    PathSoA s;
+    s.ray_o = c.take<float4>(P);
+    s.ray_d = c.take<float4>(P);
+    s.hit = c.take<float4>(P);
+    s.hit_inst = c.take<int32_t>(P);
+    s.rng = c.take<uint4>(2 * P);
+    s.beta = c.take<float4>(P);
+    s.L = c.take<float4>(P);
+    s.aov_a = c.take<float4>(P);
+    s.aov_n = c.take<float4>(P);
+    s.pend = c.take<float4>(P * ns);
+    s.sh_o = c.take<float4>(P * ns);
+    s.sh_d = c.take<float4>(P * ns);
+    s.q[0] = c.take<uint32_t>(P);
+    s.q[1] = c.take<uint32_t>(P);
+    s.sq = c.take<uint32_t>(P * ns);
+    s.acc_r = c.take<float4>(npix);
+    s.acc_a = c.take<float4>(npix);
+    s.acc_n = c.take<float4>(npix);
+    s.ctl = c.take<WaveCtl>(1);
+    if (out) *out = s;
+    return c.off + 256;
+}
+
+DevCamera make_camera(const pyre_camera_desc& c) {
+    // PinholeCamera / ThinLensCamera::look_at (camera.rs:49-72, 105-122) on the host.
+    DevCamera d;
+    f3 origin = mk3(c.origin[0], c.origin[1], c.origin[2]);
+    f3 target = mk3(c.target[0], c.target[1], c.target[2]);
+    f3 up = mk3(c.up[0], c.up[1], c.up[2]);
+    d.origin = origin;
+    d.forward = normalize3(target - origin);
+    d.right = normalize3(cross3(d.forward, up));
+    d.up = cross3(d.right, d.forward);
+    const float to_rad = 3.14159265358979323846f / 180.0f;
+    d.half_height = std::tan(c.vfov_deg * to_rad / 2.0f);
+    d.half_width = c.aspect * d.half_height;
+    d.aperture_radius = c.aperture_radius;
+    d.focus_distance = c.focus_distance;
+    d.thin_lens = c.kind == PYRE_CAMERA_THIN_LENS ? 1 : 0;
+    return d;
+}
+
+struct Launch {
+    int block_stage = 256;
+    int grid_raygen, grid_shade, grid_extend, grid_shadow, grid_acc;
+};
+
+// Stage timing (off by default): an event before each stage kernel, tagged
+// with that kernel's stage; durations are differences of consecutive events.
+void mark(pyre_ctx* ctx, int tag) {
+    if (!ctx->stage_timing) return;
+    if (ctx->stage_used == ctx->stage_ev.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        ctx->stage_ev.push_back(e);
+        ctx->stage_tag.push_back(0);
+    }
+    ctx->stage_tag[ctx->stage_used] = tag;
+    cudaEventRecord(ctx->stage_ev[ctx->stage_used++], ctx->stream);
+}
+
+enum { STAGE_EXTEND = 0, STAGE_SHADE = 1, STAGE_SHADOW = 2, STAGE_OTHER = 3, STAGE_END = 4 };
+
+void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const WaveParams& W, const Launch& Lc) {
+    cudaStream_t st = ctx->stream;
+    mark(ctx, STAGE_OTHER);
+    k_wave_begin<<<1, 32, 0, st>>>(P.ctl, W.spp_begin, W.spp_end, W.k_per_wave, W.npix);
+    k_raygen<<<Lc.grid_raygen, 256, 0, st>>>(P, W);
+    for (uint32_t d = 0; d < W.max_depth; ++d) {
+        mark(ctx, STAGE_EXTEND);
+        k_extend<<<Lc.grid_extend, 128, 0, st>>>(S, P, d);
+        mark(ctx, STAGE_SHADE);
+        k_shade<<<Lc.grid_shade, 256, 0, st>>>(S, P, W, d);
+        if (W.ns > 0) {
+            mark(ctx, STAGE_SHADOW);
+            k_shadow<<<Lc.grid_shadow, 128, 0, st>>>(S, P, d);
+        }
+    }
+    mark(ctx, STAGE_OTHER);
+    k_accumulate<<<Lc.grid_acc, 256, 0, st>>>(P, W);
+    k_wave_end<<<1, 32, 0, st>>>(P.ctl, W.max_depth);
+    mark(ctx, STAGE_END);
+}
+
+uint32_t kernels_per_wave(const WaveParams& W) { return 4 + W.max_depth * (W.ns > 0 ? 3 : 2); }
+
+}  // namespace
+}  // namespace pyre
+
+using namespace pyre;
+
+extern "C" {
+
+int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                const pyre_render_params* params, pyre_film* film) {
+    if (!ctx || !scene || !camera || !params || !film)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_render: NULL argument");
+    cudaSetDevice(ctx->device);
+    const pyre_render_params& rp = *params;
+    if (rp.width == 0 || rp.height == 0) return set_error(ctx, PYRE_ERR_INVALID, "image size is zero");
+    if (rp.spp_end <= rp.spp_begin) return set_error(ctx, PYRE_ERR_INVALID, "empty sample range");
+    if (rp.max_depth > PYRE_MAX_DEPTH) return set_error(ctx, PYRE_ERR_INVALID, "max_depth above 64");
+    uint32_t x0 = rp.crop[0], y0 = rp.crop[1], x1 = rp.crop[2], y1 = rp.crop[3];
+    if (x0 == 0 && y0 == 0 && x1 == 0 && y1 == 0) { x1 = rp.width; y1 = rp.height; }
+    if (x1 > rp.width || y1 > rp.height || x0 >= x1 || y0 >= y1)
+        return set_error(ctx, PYRE_ERR_INVALID, "crop outside the image");
+    if (camera->kind > PYRE_CAMERA_THIN_LENS) return set_error(ctx, PYRE_ERR_INVALID, "unknown camera kind");
+    if (film->mem != PYRE_MEM_HOST && film->mem != PYRE_MEM_DEVICE)
+        return set_error(ctx, PYRE_ERR_INVALID, "film.mem must be PYRE_MEM_HOST or PYRE_MEM_DEVICE");
+
+    WaveParams W;
+    std::memset(&W, 0, sizeof W);
+    W.cam = make_camera(*camera);
+    W.width = rp.width; W.height = rp.height;
+    W.cx0 = x0; W.cy0 = y0; W.cw = x1 - x0; W.ch = y1 - y0;
+    W.npix = W.cw * W.ch;
+    W.spp_begin = rp.spp_begin; W.spp_end = rp.spp_end;
+    W.max_depth = rp.max_depth; W.min_rr = rp.min_rr_depth;
+    W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
+    W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
+    const uint32_t spp = rp.spp_end - rp.spp_begin;
+    uint64_t target = rp.wave_paths ? rp.wave_paths : (uint64_t)8 << 20;
+    uint64_t K = std::max<uint64_t>(1, target / W.npix);
+    K = std::min<uint64_t>(K, spp);
+    if ((uint64_t)W.npix * K > (uint64_t)1 << 31) K = std::max<uint64_t>(1, ((uint64_t)1 << 31) / W.npix);
+    W.k_per_wave = (uint32_t)K;
+    const size_t P = (size_t)W.npix * K;
+    const uint32_t waves = (uint32_t)((spp + K - 1) / K);
+
+    size_t film_bytes = (size_t)W.npix * 10 * sizeof(float);
+    size_t need = carve_paths(nullptr, P, std::max(W.ns, 1u), W.npix, nullptr);
+    int rc = ensure_workspace(ctx, ctx->render_ws, need);
+    if (rc) return rc;
+    PathSoA S;
+    carve_paths((char*)ctx->render_ws.ptr, P, std::max(W.ns, 1u), W.npix, &S);
+    if (film->mem == PYRE_MEM_HOST && (rc = ensure_workspace(ctx, ctx->io_ws, film_bytes))) return rc;
+
+    Launch Lc;
+    Lc.grid_raygen = grid_for(ctx, k_raygen, 256);
+    Lc.grid_shade = grid_for(ctx, k_shade, 256);
+    Lc.grid_extend = grid_for(ctx, k_extend, 128);
+    Lc.grid_shadow = grid_for(ctx, k_shadow, 128);
+    Lc.grid_acc = grid_for(ctx, k_accumulate, 256);
+
+    cudaStream_t st = ctx->stream;
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_r, 0, (size_t)W.npix * sizeof(float4), st));
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_a, 0, (size_t)W.npix * sizeof(float4), st));
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_n, 0, (size_t)W.npix * sizeof(float4), st));
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
+
+    const DevScene& D = scene->dev;
+    ctx->stage_used = 0;
+    if (rp.use_graph && !ctx->stage_timing) {
+        // One wave captured once per configuration, replayed `waves` times.
+        char key[256];
+        std::snprintf(key, sizeof key, "%llu/%p/%u/%u/%u/%u/%u/%u/%u/%u/%d", (unsigned long long)scene->serial, ctx->render_ws.ptr,
+                      W.npix, W.k_per_wave, W.max_depth, W.min_rr, W.ns, W.spp_begin, W.spp_end, W.cx0 + W.cy0 * 65536u,
+                      W.env_cdf);
+        std::string k2 = std::string(key) + "/" + std::to_string(W.width) + "x" + std::to_string(W.height);
+        // camera bytes are part of the key
+        k2.append(reinterpret_cast<const char*>(&W.cam), sizeof(W.cam));
+        if (!ctx->wave_graph || ctx->wave_graph_key != k2) {
+            if (ctx->wave_graph) { cudaGraphExecDestroy(ctx->wave_graph); ctx->wave_graph = nullptr; }
+            cudaGraph_t g;
+            PYRE_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            enqueue_wave(ctx, D, S, W, Lc);
+            PYRE_CUDA_TRY(ctx, cudaStreamEndCapture(st, &g));
+            cudaError_t e = cudaGraphInstantiate(&ctx->wave_graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { ctx->wave_graph = nullptr; return cuda_check(ctx, e, "cudaGraphInstantiate"); }
+            ctx->wave_graph_key = k2;
+        }
+        for (uint32_t w = 0; w < waves; ++w) PYRE_CUDA_TRY(ctx, cudaGraphLaunch(ctx->wave_graph, st));
+    } else {
+        for (uint32_t w = 0; w < waves; ++w) enqueue_wave(ctx, D, S, W, Lc);
+    }
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+
+    const float inv_spp = 1.0f / (float)spp;
+    float* out[4] = {film->radiance, film->albedo, film->normal, film->depth};
+    float* dst[4];
+    float* staging = (float*)ctx->io_ws.ptr;
+    size_t offs[4] = {0, (size_t)W.npix * 3, (size_t)W.npix * 6, (size_t)W.npix * 9};
+    for (int c = 0; c < 4; ++c) dst[c] = out[c] ? (film->mem == PYRE_MEM_HOST ? staging + offs[c] : out[c]) : nullptr;
+    k_finalize<<<Lc.grid_acc, 256, 0, st>>>(S, W.npix, inv_spp, dst[0], dst[1], dst[2], dst[3]);
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[1], st));
+    if (film->mem == PYRE_MEM_HOST) {
+        for (int c = 0; c < 4; ++c)
+            if (out[c])
+                PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(out[c], dst[c], (c == 3 ? 1 : 3) * (size_t)W.npix * sizeof(float),
+                                                   cudaMemcpyDeviceToHost, st));
+    }
+    WaveCtl ctl;
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(&ctl, S.ctl, sizeof ctl, cudaMemcpyDeviceToHost, st));
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    if ((rc = take_kernel_error(ctx))) return rc;
+    pyre_render_stats& s = ctx->stats;
+    std::memset(&s, 0, sizeof s);
+    s.samples = ctl.samples;
+    s.extend_rays = ctl.extend_rays;
+    s.shadow_rays = ctl.shadow_rays;
+    s.waves = waves;
+    s.kernel_launches = waves * kernels_per_wave(W) + 1;
+    cudaEventElapsedTime(&s.ms_total, ctx->ev[0], ctx->ev[1]);
+    if (ctx->stage_timing) {
+        float acc[4] = {0, 0, 0, 0};
+        for (size_t k = 0; k + 1 < ctx->stage_used; ++k) {
+            int tag = ctx->stage_tag[k];
+            if (tag > STAGE_OTHER) continue;
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ctx->stage_ev[k], ctx->stage_ev[k + 1]);
+            acc[tag] += ms;
+        }
+        s.ms_extend = acc[STAGE_EXTEND];
+        s.ms_shade = acc[STAGE_SHADE];
+        s.ms_shadow = acc[STAGE_SHADOW];
+        s.ms_other = acc[STAGE_OTHER];
+    }
+    return PYRE_OK;
+}
+
+static int intersect_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_rays* rays, uint64_t n, pyre_hits* hits,
+                          uint8_t* occluded, int mem, bool any) {
+    if (!ctx || !scene || !rays) return set_error(ctx, PYRE_ERR_INVALID, "intersect: NULL argument");
+    if (!rays->origin || !rays->direction || !rays->t_min || !rays->t_max)
+        return set_error(ctx, PYRE_ERR_INVALID, "intersect: ray arrays missing");
+    if (any ? !occluded : (!hits || !hits->kind || !hits->instance || !hits->triangle || !hits->t || !hits->u || !hits->v))
+        return set_error(ctx, PYRE_ERR_INVALID, "intersect: output arrays missing");
+    if (mem != PYRE_MEM_HOST && mem != PYRE_MEM_DEVICE) return set_error(ctx, PYRE_ERR_INVALID, "intersect: bad mem");
+    if (n == 0) return PYRE_OK;
+    if (n > 0x7fffffffull) return set_error(ctx, PYRE_ERR_INVALID, "intersect: more than 2^31-1 rays");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    const float *org = rays->origin, *dir = rays->direction, *tmin = rays->t_min, *tmax = rays->t_max,
+                *time = rays->time;
+    int32_t *kind = nullptr, *inst = nullptr, *tri = nullptr;
+    float *tt = nullptr, *uu = nullptr, *vv = nullptr;
+    uint8_t* occ = occluded;
+    if (!any) { kind = hits->kind; inst = hits->instance; tri = hits->triangle; tt = hits->t; uu = hits->u; vv = hits->v; }
+    if (mem == PYRE_MEM_HOST) {
+        size_t in_bytes = n * (time ? 9 : 8) * sizeof(float);
+        size_t out_bytes = any ? n : n * 6 * sizeof(float);
+        int rc = ensure_workspace(ctx, ctx->io_ws, in_bytes + out_bytes + 1024);
+        if (rc) return rc;
+        char* b = (char*)ctx->io_ws.ptr;
+        float* d_org = (float*)b;
+        float* d_dir = d_org + 3 * n;
+        float* d_tmin = d_dir + 3 * n;
+        float* d_tmax = d_tmin + n;
+        float* d_time = time ? d_tmax + n : nullptr;
+        char* ob = (char*)(d_tmax + n + (time ? n : 0));
+        PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(d_org, org, 3 * n * sizeof(float), cudaMemcpyHostToDevice, st));
+        PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(d_dir, dir, 3 * n * sizeof(float), cudaMemcpyHostToDevice, st));
+        PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(d_tmin, tmin, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(d_tmax, tmax, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        if (time) PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(d_time, time, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        org = d_org; dir = d_dir; tmin = d_tmin; tmax = d_tmax; time = d_time;
+        if (any) occ = (uint8_t*)ob;
+        else {
+            kind = (int32_t*)ob; inst = kind + n; tri = inst + n;
+            tt = (float*)(tri + n); uu = tt + n; vv = uu + n;
+        }
+    }
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), st));
+    if (any) {
+        int grid = grid_for(ctx, k_intersect<true>, 128);
+        k_intersect<true><<<grid, 128, 0, st>>>(scene->dev, org, dir, tmin, tmax, time, (uint32_t)n, ctx->d_counter,
+                                                nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, occ);
+    } else {
+        int grid = grid_for(ctx, k_intersect<false>, 128);
+        k_intersect<false><<<grid, 128, 0, st>>>(scene->dev, org, dir, tmin, tmax, time, (uint32_t)n, ctx->d_counter,
+                                                 kind, inst, tri, tt, uu, vv, nullptr);
+    }
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    if (mem == PYRE_MEM_HOST) {
+        if (any) PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(occluded, occ, n, cudaMemcpyDeviceToHost, st));
+        else {
+            PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(hits->kind, kind, n * 4, cudaMemcpyDeviceToHost, st));
+            PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(hits->instance, inst, n * 4, cudaMemcpyDeviceToHost, st));
+            PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(hits->triangle, tri, n * 4, cudaMemcpyDeviceToHost, st));
+            PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(hits->t, tt, n * 4, cudaMemcpyDeviceToHost, st));
+            PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(hits->u, uu, n * 4, cudaMemcpyDeviceToHost, st));
+            PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(hits->v, vv, n * 4, cudaMemcpyDeviceToHost, st));
+        }
+    }
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    return take_kernel_error(ctx);
+}
+
+int pyre_intersect_closest(pyre_ctx* ctx, const pyre_scene* scene, const pyre_rays* rays, uint64_t n, pyre_hits* hits,
+                           int mem) {
+    return intersect_impl(ctx, scene, rays, n, hits, nullptr, mem, false);
+}
+
+int pyre_intersect_any(pyre_ctx* ctx, const pyre_scene* scene, const pyre_rays* rays, uint64_t n, uint8_t* occluded,
+                       int mem) {
+    return intersect_impl(ctx, scene, rays, n, nullptr, occluded, mem, true);
+}
+
+}  // extern "C"

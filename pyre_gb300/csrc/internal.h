@@ -1,0 +1,60 @@
+// internal.h — context and scene objects behind the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+#include "../../include/pyre_cuda.h"
+#include "device_scene.cuh"
+
+struct pyre_scene {
+    pyre::DevScene dev;
+    uint64_t serial = 0;  // unique per upload; keys cached CUDA graphs
+    std::vector<void*> allocations;  // device buffers owned by the scene
+    std::vector<int32_t> slot_of_instance;  // original instance id -> device slot
+    uint32_t n_triangles = 0;
+    uint64_t n_nodes = 0;
+    uint64_t device_bytes = 0;
+};
+
+// Reusable device workspace of a context (grown on demand, freed at destroy).
+struct Workspace {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct pyre_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string error;
+    int* d_error = nullptr;     // kernel-reported status (PYRE_ERR_OVERFLOW ...)
+    unsigned int* d_counter = nullptr;  // work counter of the intersect kernels
+    Workspace render_ws;        // path state of the wavefront integrator
+    Workspace io_ws;            // staging for host-memory rays / films
+    pyre_render_stats stats{};
+    int stage_timing = 0;
+    cudaEvent_t ev[16] = {};
+    // Stage timing: one event between consecutive stage kernels, with the
+    // stage (0 extend, 1 shade, 2 shadow, 3 other) of the kernel that follows.
+    std::vector<cudaEvent_t> stage_ev;
+    std::vector<int> stage_tag;
+    size_t stage_used = 0;
+    // CUDA graph of one wave, keyed by the render configuration it was captured for.
+    cudaGraphExec_t wave_graph = nullptr;
+    std::string wave_graph_key;
+};
+
+namespace pyre {
+int set_error(pyre_ctx* ctx, int code, const std::string& msg);
+int cuda_check(pyre_ctx* ctx, cudaError_t e, const char* what);
+// Grows `ws` to at least `bytes` (contents not preserved).
+int ensure_workspace(pyre_ctx* ctx, Workspace& ws, size_t bytes);
+// Reads and clears the kernel error flag; returns its status.
+int take_kernel_error(pyre_ctx* ctx);
+}  // namespace pyre
+
+#define PYRE_CUDA_TRY(ctx, expr)                                   \
+    do {                                                           \
+        cudaError_t _e = (expr);                                   \
+        if (_e != cudaSuccess) return pyre::cuda_check(ctx, _e, #expr); \
+    } while (0)
