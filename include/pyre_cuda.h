@@ -254,6 +254,27 @@ typedef struct pyre_render_stats {
 int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
                 const pyre_render_params* params, pyre_film* film);
 int pyre_get_render_stats(const pyre_ctx* ctx, pyre_render_stats* out);
+
+/* Render without allocating. No counterpart in the reference: this entry
+ * point exists for callers that cannot call cudaMalloc while they render,
+ * e.g. a host application whose GPU memory belongs to its own allocator, or a
+ * frame loop that must not stall the device (cudaMalloc can synchronise it).
+ * It runs the same kernels as pyre_render, but the path state lives in one
+ * file-scope static device array of PYRE_NOALLOC_SCRATCH_BYTES (32 MiB), held
+ * by every GPU that loads the library until the process exits, and the film
+ * must be caller-owned device memory (film->mem == PYRE_MEM_DEVICE).
+ * Limits: the crop (x1-x0)*(y1-y0) must fit the array with one sample per
+ * pixel (PYRE_ERR_INVALID names the largest pixel count for the scene's light
+ * count otherwise); render larger images as crop tiles. No CUDA graph
+ * replay; stage timing is ignored.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. Every call on a device shares the one array and
+ * leaves its contents behind (each call clears what must start at zero):
+ * calls that overlap on the GPU, from two contexts or two threads, race. */
+#define PYRE_NOALLOC_SCRATCH_BYTES (32u << 20)
+int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                        const pyre_render_params* params, pyre_film* film);
 /* Per-stage timing with CUDA events (adds synchronisation; off by default). */
 int pyre_set_stage_timing(pyre_ctx* ctx, int enabled);
 

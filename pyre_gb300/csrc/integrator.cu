@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "internal.h"
@@ -707,6 +708,129 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
     }
     return PYRE_OK;
 }
+
+}  // extern "C"
+
+// --------------------------------------------------- render without malloc --
+// Path state for pyre_render_noalloc: one static array per device that loads
+// the library, used in place of the context's cudaMalloc'd workspace.
+namespace pyre {
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PYRE_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {};
+
+// Device address of the static array on ctx->device (looked up once per
+// device, with that device current).
+int noalloc_scratch(pyre_ctx* ctx, void** out) {
+    if (ctx->device < 0 || ctx->device >= 256) return set_error(ctx, PYRE_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[ctx->device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_check(ctx, e, "cudaGetSymbolAddress(noalloc scratch)");
+        g_noalloc_addr[ctx->device] = p;
+    }
+    *out = g_noalloc_addr[ctx->device];
+    return PYRE_OK;
+}
+}  // namespace
+}  // namespace pyre
+
+extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                                   const pyre_render_params* params, pyre_film* film) {
+    if (!ctx || !scene || !camera || !params || !film)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_noalloc: NULL argument");
+    PYRE_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const pyre_render_params& rp = *params;
+    if (film->mem != PYRE_MEM_DEVICE)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_noalloc: the film must be device memory");
+    if (rp.width == 0 || rp.height == 0) return set_error(ctx, PYRE_ERR_INVALID, "image size is zero");
+    if (rp.spp_end <= rp.spp_begin) return set_error(ctx, PYRE_ERR_INVALID, "empty sample range");
+    if (rp.max_depth > PYRE_MAX_DEPTH) return set_error(ctx, PYRE_ERR_INVALID, "max_depth above 64");
+    uint32_t x0 = rp.crop[0], y0 = rp.crop[1], x1 = rp.crop[2], y1 = rp.crop[3];
+    if (x0 == 0 && y0 == 0 && x1 == 0 && y1 == 0) { x1 = rp.width; y1 = rp.height; }
+    if (x1 > rp.width || y1 > rp.height || x0 >= x1 || y0 >= y1)
+        return set_error(ctx, PYRE_ERR_INVALID, "crop outside the image");
+    if (camera->kind > PYRE_CAMERA_THIN_LENS) return set_error(ctx, PYRE_ERR_INVALID, "unknown camera kind");
+
+    WaveParams W;
+    std::memset(&W, 0, sizeof W);
+    W.cam = make_camera(*camera);
+    W.width = rp.width; W.height = rp.height;
+    W.cx0 = x0; W.cy0 = y0; W.cw = x1 - x0; W.ch = y1 - y0;
+    W.npix = W.cw * W.ch;
+    W.spp_begin = rp.spp_begin; W.spp_end = rp.spp_end;
+    W.max_depth = rp.max_depth; W.min_rr = rp.min_rr_depth;
+    W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
+    W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
+    const uint32_t ns = std::max(W.ns, 1u);
+    const size_t cap = PYRE_NOALLOC_SCRATCH_BYTES;
+    if (carve_paths(nullptr, W.npix, ns, W.npix, nullptr) > cap) {
+        uint64_t lo = 1, hi = W.npix;  // largest pixel count that fits one sample per pixel
+        while (lo < hi) {
+            uint64_t mid = (lo + hi + 1) / 2;
+            if (carve_paths(nullptr, mid, ns, (uint32_t)mid, nullptr) <= cap) lo = mid; else hi = mid - 1;
+        }
+        return set_error(ctx, PYRE_ERR_INVALID,
+                         "pyre_render_noalloc: crop of " + std::to_string(W.npix) + " pixels exceeds the " +
+                             std::to_string(cap >> 20) + " MiB static path-state array (at most " +
+                             std::to_string(lo) + " pixels with " + std::to_string(W.ns) +
+                             " NEE slots per path); render the image as smaller crop tiles");
+    }
+    const uint32_t spp = rp.spp_end - rp.spp_begin;
+    uint64_t target = rp.wave_paths ? rp.wave_paths : (uint64_t)8 << 20;
+    uint64_t K = std::min<uint64_t>(std::max<uint64_t>(1, target / W.npix), spp);
+    while (K > 1 && carve_paths(nullptr, (size_t)W.npix * K, ns, W.npix, nullptr) > cap) --K;
+    W.k_per_wave = (uint32_t)K;
+    const uint32_t waves = (uint32_t)((spp + K - 1) / K);
+
+    void* scratch = nullptr;
+    int rc = noalloc_scratch(ctx, &scratch);
+    if (rc) return rc;
+    PathSoA S;
+    carve_paths((char*)scratch, (size_t)W.npix * K, ns, W.npix, &S);
+
+    Launch Lc;
+    Lc.grid_raygen = grid_for(ctx, k_raygen, 256);
+    Lc.grid_shade = grid_for(ctx, k_shade, 256);
+    Lc.grid_extend = grid_for(ctx, k_extend, 128);
+    Lc.grid_shadow = grid_for(ctx, k_shadow, 128);
+    Lc.grid_acc = grid_for(ctx, k_accumulate, 256);
+
+    cudaStream_t st = ctx->stream;
+    // The array keeps the previous call's contents: clear the sums and counters.
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_r, 0, (size_t)W.npix * sizeof(float4), st));
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_a, 0, (size_t)W.npix * sizeof(float4), st));
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_n, 0, (size_t)W.npix * sizeof(float4), st));
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
+    const int timing = ctx->stage_timing;
+    ctx->stage_timing = 0;  // stage timing would create events
+    for (uint32_t w = 0; w < waves; ++w) enqueue_wave(ctx, scene->dev, S, W, Lc);
+    ctx->stage_timing = timing;
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    k_finalize<<<Lc.grid_acc, 256, 0, st>>>(S, W.npix, 1.0f / (float)spp, film->radiance, film->albedo, film->normal,
+                                              film->depth);
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[1], st));
+    WaveCtl ctl;
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(&ctl, S.ctl, sizeof ctl, cudaMemcpyDeviceToHost, st));
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    if ((rc = take_kernel_error(ctx))) return rc;
+    pyre_render_stats& s = ctx->stats;
+    std::memset(&s, 0, sizeof s);
+    s.samples = ctl.samples;
+    s.extend_rays = ctl.extend_rays;
+    s.shadow_rays = ctl.shadow_rays;
+    s.waves = waves;
+    s.kernel_launches = waves * kernels_per_wave(W) + 1;
+    cudaEventElapsedTime(&s.ms_total, ctx->ev[0], ctx->ev[1]);
+    return PYRE_OK;
+}
+
+extern "C" {
 
 static int intersect_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_rays* rays, uint64_t n, pyre_hits* hits,
                           uint8_t* occluded, int mem, bool any) {

@@ -129,6 +129,8 @@ SIGNATURES = {
     "pyre_intersect_any": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Rays), C.c_uint64, P_u8, C.c_int]),
     "pyre_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams), C.POINTER(Film)]),
     "pyre_get_render_stats": (C.c_int, [C.c_void_p, C.POINTER(RenderStats)]),
+    "pyre_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams),
+                                      C.POINTER(Film)]),
     "pyre_set_stage_timing": (C.c_int, [C.c_void_p, C.c_int]),
 }
 
