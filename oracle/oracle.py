@@ -49,7 +49,7 @@ _SIG = {
     "orc_env_query": (None, [C.c_void_p, P_f, C.c_uint32, P_f, P_f, P_f, P_f, P_f]),
     "orc_scene_bvh_nodes": (C.c_uint32, [C.c_void_p, C.c_uint32, C.c_void_p, P_u32]),
     "orc_intersect": (None, [C.c_void_p, P_f, P_f, P_f, P_f, P_f, C.c_uint64, C.c_int, C.c_int, P_i32, P_i32, P_i32,
-                             P_f, P_f, P_f]),
+                             P_f, P_f, P_f, P_f]),
     "orc_occluded": (None, [C.c_void_p, P_f, P_f, P_f, P_f, P_f, C.c_uint64, C.c_int, P_u8]),
     "orc_camera_rays": (None, [P_f, C.c_uint32, C.c_uint32, P_u32, C.c_uint32, P_f, P_f, P_f]),
     "orc_render": (C.c_uint64, [C.c_void_p, P_f, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
@@ -228,15 +228,18 @@ class OracleScene:
         lib().orc_scene_bvh_nodes(self.h, prim, nodes.ctypes.data_as(C.c_void_p), None)
         return nodes
 
-    def intersect(self, org, dirs, tmin, tmax, time=None, canonical=True):
+    def intersect(self, org, dirs, tmin, tmax, time=None, canonical=True, normals=False):
         org, dirs, tmin, tmax = _c(org), _c(dirs), _c(tmin), _c(tmax)
         n = tmin.size
         t_ = _c(time) if time is not None else None
         out = {k: np.zeros(n, np.int32) for k in ("kind", "instance", "triangle")}
         out.update({k: np.zeros(n, F32) for k in ("t", "u", "v")})
+        if normals:
+            out["normal"] = np.zeros((n, 3), F32)
         lib().orc_intersect(self.h, _f(org), _f(dirs), _f(tmin), _f(tmax), _f(t_), n, 1 if canonical else 0,
                             self.nthreads, out["kind"].ctypes.data_as(P_i32), out["instance"].ctypes.data_as(P_i32),
-                            out["triangle"].ctypes.data_as(P_i32), _f(out["t"]), _f(out["u"]), _f(out["v"]))
+                            out["triangle"].ctypes.data_as(P_i32), _f(out["t"]), _f(out["u"]), _f(out["v"]),
+                            _f(out.get("normal")))
         return out
 
     def occluded(self, org, dirs, tmin, tmax, time=None):

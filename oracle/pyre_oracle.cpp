@@ -1231,7 +1231,7 @@ uint32_t orc_scene_bvh_nodes(void* s, uint32_t prim, void* nodes_out, uint32_t* 
 // Closest: kind_out 0 = miss, 1 = surface, 2 = light; inst_out = instance or light id.
 void orc_intersect(void* s, const float* org, const float* dir, const float* tmin, const float* tmax, const float* time,
                    uint64_t n, int canonical, int nthreads, int32_t* kind_out, int32_t* inst_out, int32_t* tri_out,
-                   float* t_out, float* u_out, float* v_out) {
+                   float* t_out, float* u_out, float* v_out, float* normal_out) {
     Scene* sc = (Scene*)s;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -1246,6 +1246,7 @@ void orc_intersect(void* s, const float* org, const float* dir, const float* tmi
             kind_out[i] = h.is_light ? 2 : 1; inst_out[i] = (int32_t)h.id;
             tri_out[i] = h.is_light ? -1 : (int32_t)h.hit.tri;
             t_out[i] = h.hit.t; u_out[i] = h.hit.u; v_out[i] = h.hit.v;
+            if (normal_out) { normal_out[3 * i] = h.hit.normal.x; normal_out[3 * i + 1] = h.hit.normal.y; normal_out[3 * i + 2] = h.hit.normal.z; }
         } else {
             kind_out[i] = 0; inst_out[i] = -1; tri_out[i] = -1; t_out[i] = INF; u_out[i] = 0; v_out[i] = 0;
         }

@@ -1,0 +1,36 @@
+"""Sample-range sharding of one frame across ranks (one process per GPU).
+
+Every sample is seeded by pixel_seed(x, y, s) (crates/pyre/src/sampler.rs:41-49),
+so rank r can render samples [base + r*k, base + (r+1)*k) of the same frame
+independently; there is no exchange on the data path. The per-rank films
+(means over k samples) combine into the frame's mean with one sum-reduction
+after rendering, outside any timed region.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def sample_range(rank: int, spp_per_rank: int, spp_base: int = 0) -> tuple[int, int]:
+    start = spp_base + rank * spp_per_rank
+    return start, start + spp_per_rank
+
+
+def reduce_film_means(channels: dict, count: int, group=None) -> dict:
+    """Combines per-rank per-pixel means of `count` samples into global means.
+
+    `channels` maps names to numpy arrays (or torch tensors); works with any
+    torch.distributed backend (gloo on CPU, NCCL on GPU tensors).
+    """
+    import torch
+    import torch.distributed as dist
+
+    out = {}
+    n = torch.tensor([float(count)], dtype=torch.float64)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM, group=group)
+    for name, arr in channels.items():
+        t = torch.as_tensor(np.asarray(arr) if not isinstance(arr, torch.Tensor) else arr).to(torch.float64)
+        t = t * float(count)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+        out[name] = (t / n.item()).to(torch.float32).numpy() if t.device.type == "cpu" else t / n.item()
+    return out
