@@ -41,6 +41,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Msamples/s @1080p depth 8"
 UNIT = "Msamples/s"
 W, H, SPP, DEPTH, RR = 1920, 1080, 64, 8, 3
+# CPU sample: every third image row at full spp (about 10-15 s on 16 cores)
+CPU_ROWS = 360
 
 
 def parse():
@@ -131,7 +133,7 @@ def run_reference(args):
     O.lib()
     scene, cam, _ = make_workload()
     threads = os.cpu_count() or 1
-    rows = args.cpu_rows or 8
+    rows = args.cpu_rows or CPU_ROWS
     for _ in range(args.warmup):
         cpu_sample(scene, cam, max(1, rows // 4), threads)
     vals, times = [], []
@@ -286,7 +288,7 @@ def main():
             "roofline": roofline}
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rows = args.cpu_rows or 8
+        rows = args.cpu_rows or CPU_ROWS
         v, dt, n = cpu_sample(scene, cam, rows, threads)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{rows} rows x 1920 px at 64 spp ({n} samples, {dt:.1f} s); C++ "

@@ -125,137 +125,154 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
                  clampf_(time, 0.0f, 1.0f));
 }
 
-// Traverses one instance's BVH. Closest: tightens *best_t and records the hit
-// with the canonical tie rule. Any: returns true on the first admissible hit.
-template <bool ANY>
-__device__ __forceinline__ bool trace_blas(const DevScene& S, const DevInstance& I, int32_t islot, const TraceRay& r,
-                                           const f3& inv, float* best_t, TraceHit* hit, uint32_t* best_key_tri,
-                                           int* stack) {
-    f3 o = r.o;
-    if (I.has_motion) {
-        f3 off = motion_offset(I, r.time);
-        if (!is_zero3(off)) o = r.o - off;
-    }
-    float entry;
-    if (!slab(I.lo[0], I.hi[0], I.lo[1], I.hi[1], I.lo[2], I.hi[2], o, inv, r.tmin, *best_t, &entry)) return false;
-    int sp = 0;
-    int node = I.blas_root;
-    while (true) {
-        const float4* N = S.nodes + 4 * (size_t)node;
-        const float4 na = __ldg(N), nb = __ldg(N + 1), nc = __ldg(N + 2);
-        const int4 nd = __ldg(reinterpret_cast<const int4*>(N + 3));
-        float e0, e1;
-        bool h0 = nd.x >= 0 && slab(na.x, na.y, na.z, na.w, nc.x, nc.y, o, inv, r.tmin, *best_t, &e0);
-        bool h1 = nd.y >= 0 && slab(nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, o, inv, r.tmin, *best_t, &e1);
-        // Leaves are tested in place; interior children are followed.
-        int kids[2] = {nd.x, nd.y};
-        int counts[2] = {nd.z, nd.w};
-        bool go[2] = {false, false};
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            bool hc = c == 0 ? h0 : h1;
-            if (!hc) continue;
-            if (counts[c] > 0) {
-                for (int k = kids[c]; k < kids[c] + counts[c]; ++k) {
-                    const float4 A = __ldg(S.tris + 3 * (size_t)k), B = __ldg(S.tris + 3 * (size_t)k + 1),
-                                 C = __ldg(S.tris + 3 * (size_t)k + 2);
-                    float t, u, v;
-                    if (!mt_test(o, r.d, A, B, C, &t, &u, &v)) continue;
-                    if (!(t > r.tmin && t < r.tmax)) continue;
-                    if (ANY) return true;
-                    const uint32_t key = __float_as_uint(A.w);
-                    bool better = t < *best_t;
-                    if (!better && t == *best_t && hit->inst >= 0) {
-                        const int32_t oi = I.orig_id, ob = S.inst[hit->inst].orig_id;
-                        better = oi < ob || (oi == ob && key < *best_key_tri);
-                    }
-                    if (better) {
-                        *best_t = t;
-                        hit->t = t; hit->u = u; hit->v = v;
-                        hit->inst = islot; hit->tri = k;
-                        *best_key_tri = key;
-                    }
-                }
-            } else {
-                go[c] = true;
-            }
-        }
-        if (go[0] && go[1]) {
-            // nearer child next, farther one on the stack
-            int nearc = e0 <= e1 ? kids[0] : kids[1];
-            int farc = e0 <= e1 ? kids[1] : kids[0];
-            if (sp >= PYRE_STACK) { atomicExch(S.error_flag, -5); return false; }
-            stack[sp++] = farc;
-            node = nearc;
-        } else if (go[0]) {
-            node = kids[0];
-        } else if (go[1]) {
-            node = kids[1];
-        } else {
-            if (sp == 0) break;
-            node = stack[--sp];
-        }
-    }
-    return false;
-}
+// Warp-synchronous two-level traversal (top-level BVH over instances, then
+// each reached instance's BVH), equivalent to the instance scan of
+// Scene::intersect / Scene::occluded (scene.rs:57-140): closest hit with the
+// canonical tie rule, or any hit.
+//
+// All 32 lanes of the warp must call it (lanes without a ray pass
+// valid = false). Each lane keeps one tagged stack:
+//   [0, 2^29)          node of an instance BVH
+//   TOP | n            node of the top-level BVH
+//   INST | slot        enter instance `slot` (root-box test, local origin)
+//   EXIT               leave the current instance (restore the world origin)
+// Inner nodes are stepped while any lane of the warp still needs a leaf; a
+// lane that already holds one leaf keeps stepping speculatively. Leaves found
+// on the way are parked (at most three triangle ranges, all of the current
+// instance: a lane holding leaves does not leave or enter an instance) and
+// then tested by all lanes in lock step. An any-hit lane is marked finished
+// rather than returning, so lanes stay converged.
+#define PYRE_TAG_TOP (1 << 29)
+#define PYRE_TAG_INST (1 << 30)
+#define PYRE_NODE_NONE (-1)
+#define PYRE_NODE_EXIT (-2)
 
-// Scene traversal: the top-level BVH over instance swept bounds, then each
-// reached instance's BVH. Equivalent to the instance scan of Scene::intersect
-// / Scene::occluded (scene.rs:57-140) for closest (with the canonical tie
-// rule) and any hit.
 template <bool ANY>
-__device__ bool trace_scene(const DevScene& S, const TraceRay& r, TraceHit* hit) {
+__device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r, bool valid, TraceHit* hit) {
+    const unsigned FULL = 0xffffffffu;
     hit->inst = -1; hit->tri = -1; hit->light = -1;
     hit->t = r.tmax; hit->u = 0.0f; hit->v = 0.0f;
+    const f3 inv = mk3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
     float best_t = r.tmax;
     uint32_t best_key = 0xffffffffu;
-    const f3 inv = mk3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
+    int32_t best_orig = 0x7fffffff;
+    bool found = false;
+    // term: the lane has nothing left to do; exhausted: no node left to step
+    bool term = !valid || S.tlas_root < 0;
+    bool exhausted = term;
     int stack[PYRE_STACK];
-    if (S.tlas_root >= 0) {
-        int tstack[PYRE_STACK];
-        int tsp = 0;
-        int node = S.tlas_root;
-        while (true) {
-            const float4* N = S.nodes + 4 * (size_t)node;
+    int sp = 0;
+    int node = term ? PYRE_NODE_NONE : (S.tlas_root | PYRE_TAG_TOP);
+    int inst = -1;
+    int32_t inst_orig = 0;
+    f3 o = r.o;
+    // up to three parked triangle ranges; a lane keeps stepping (speculatively)
+    // while it holds at most one, so one node step never needs more than three
+    int ls[3] = {0, 0, 0}, lc[3] = {0, 0, 0};
+    int parked = 0;
+
+    while (__any_sync(FULL, !term)) {
+        // ---- inner phase: step nodes until every lane holds a leaf or has none left
+        while (__any_sync(FULL, !term && !exhausted && parked == 0)) {
+            if (term || exhausted || parked >= 2) continue;
+            if (node == PYRE_NODE_NONE) {
+                if (sp == 0) { exhausted = true; continue; }
+                node = stack[--sp];
+            }
+            if (node == PYRE_NODE_EXIT) {
+                if (parked) { stack[sp++] = PYRE_NODE_EXIT; node = PYRE_NODE_NONE; parked = parked < 2 ? 2 : parked; continue; }
+                inst = -1;
+                o = r.o;
+                node = PYRE_NODE_NONE;
+                continue;
+            }
+            if (node & PYRE_TAG_INST) {
+                if (parked) { stack[sp++] = node; node = PYRE_NODE_NONE; parked = parked < 2 ? 2 : parked; continue; }
+                const int k = node & ~PYRE_TAG_INST;
+                node = PYRE_NODE_NONE;
+                const DevInstance& I = S.inst[k];
+                const int root = I.blas_root;
+                if (root < 0) continue;
+                f3 lo = r.o;
+                if (I.has_motion) {
+                    f3 off = motion_offset(I, r.time);
+                    if (!is_zero3(off)) lo = r.o - off;
+                }
+                float e;
+                if (!slab(I.lo[0], I.hi[0], I.lo[1], I.hi[1], I.lo[2], I.hi[2], lo, inv, r.tmin, best_t, &e)) continue;
+                if (sp >= PYRE_STACK) { atomicExch(S.error_flag, -5); term = exhausted = true; continue; }
+                stack[sp++] = PYRE_NODE_EXIT;
+                inst = k;
+                inst_orig = I.orig_id;
+                o = lo;
+                node = root;
+                continue;
+            }
+            const bool top = (node & PYRE_TAG_TOP) != 0;
+            const float4* N = S.nodes + 4 * (size_t)(node & ~PYRE_TAG_TOP);
             const float4 na = __ldg(N), nb = __ldg(N + 1), nc = __ldg(N + 2);
             const int4 nd = __ldg(reinterpret_cast<const int4*>(N + 3));
             float e0, e1;
-            bool h0 = nd.x >= 0 && slab(na.x, na.y, na.z, na.w, nc.x, nc.y, r.o, inv, r.tmin, best_t, &e0);
-            bool h1 = nd.y >= 0 && slab(nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, r.o, inv, r.tmin, best_t, &e1);
-            int kids[2] = {nd.x, nd.y};
-            int counts[2] = {nd.z, nd.w};
-            bool go[2] = {false, false};
-            for (int c = 0; c < 2; ++c) {
-                bool hc = c == 0 ? h0 : h1;
-                if (!hc) continue;
-                if (counts[c] > 0) {
-                    for (int k = kids[c]; k < kids[c] + counts[c]; ++k) {
-                        const DevInstance I = S.inst[k];
-                        if (I.blas_root < 0) continue;
-                        if (trace_blas<ANY>(S, I, k, r, inv, &best_t, hit, &best_key, stack)) return true;
-                    }
-                } else {
-                    go[c] = true;
-                }
-            }
-            if (go[0] && go[1]) {
-                int nearc = e0 <= e1 ? kids[0] : kids[1];
-                int farc = e0 <= e1 ? kids[1] : kids[0];
-                if (tsp >= PYRE_STACK) { atomicExch(S.error_flag, -5); break; }
-                tstack[tsp++] = farc;
-                node = nearc;
-            } else if (go[0]) {
-                node = kids[0];
-            } else if (go[1]) {
-                node = kids[1];
+            const bool h0 = nd.x >= 0 && slab(na.x, na.y, na.z, na.w, nc.x, nc.y, o, inv, r.tmin, best_t, &e0);
+            const bool h1 = nd.y >= 0 && slab(nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, o, inv, r.tmin, best_t, &e1);
+            node = PYRE_NODE_NONE;
+            const bool leaf0 = nd.z > 0, leaf1 = nd.w > 0;
+            // leaves: park triangle ranges, or queue the instances of a top-level leaf
+            if (top) {
+                const int need = (h0 && leaf0 ? nd.z : 0) + (h1 && leaf1 ? nd.w : 0) + 1;
+                if (sp + need > PYRE_STACK) { atomicExch(S.error_flag, -5); term = exhausted = true; continue; }
+                if (h1 && leaf1)
+                    for (int k = nd.w - 1; k >= 0; --k) stack[sp++] = PYRE_TAG_INST | (nd.y + k);
+                if (h0 && leaf0)
+                    for (int k = nd.z - 1; k >= 0; --k) stack[sp++] = PYRE_TAG_INST | (nd.x + k);
             } else {
-                if (tsp == 0) break;
-                node = tstack[--tsp];
+                if (h0 && leaf0) { ls[parked] = nd.x; lc[parked] = nd.z; ++parked; }
+                if (h1 && leaf1) { ls[parked] = nd.y; lc[parked] = nd.w; ++parked; }
+            }
+            const int tag = top ? PYRE_TAG_TOP : 0;
+            const bool g0 = h0 && !leaf0, g1 = h1 && !leaf1;
+            if (g0 && g1) {
+                const bool first0 = e0 <= e1;
+                if (sp >= PYRE_STACK) { atomicExch(S.error_flag, -5); term = exhausted = true; continue; }
+                stack[sp++] = (first0 ? nd.y : nd.x) | tag;
+                node = (first0 ? nd.x : nd.y) | tag;
+            } else if (g0) {
+                node = nd.x | tag;
+            } else if (g1) {
+                node = nd.y | tag;
             }
         }
+        // ---- leaf phase: all lanes test their parked triangles together
+        const int c0 = term ? 0 : lc[0], c1 = term ? 0 : lc[1], c2 = term ? 0 : lc[2];
+        const int total = parked == 0 ? 0 : c0 + (parked > 1 ? c1 : 0) + (parked > 2 ? c2 : 0);
+        const int kmax = __reduce_max_sync(FULL, total);
+        for (int k = 0; k < kmax; ++k) {
+            if (k >= total || term) continue;
+            const int slot = k < c0 ? ls[0] + k : (k < c0 + c1 ? ls[1] + (k - c0) : ls[2] + (k - c0 - c1));
+            const float4 A = __ldg(S.tris + 3 * (size_t)slot), B = __ldg(S.tris + 3 * (size_t)slot + 1),
+                         C = __ldg(S.tris + 3 * (size_t)slot + 2);
+            float t, u, v;
+            if (!mt_test(o, r.d, A, B, C, &t, &u, &v)) continue;
+            if (!(t > r.tmin && t < r.tmax)) continue;
+            if (ANY) { found = true; term = true; continue; }
+            const uint32_t key = __float_as_uint(A.w);
+            bool better = t < best_t;
+            if (!better && t == best_t && found)
+                better = inst_orig < best_orig || (inst_orig == best_orig && key < best_key);
+            if (better) {
+                best_t = t;
+                found = true;
+                hit->t = t; hit->u = u; hit->v = v;
+                hit->inst = inst; hit->tri = slot;
+                best_key = key;
+                best_orig = inst_orig;
+            }
+        }
+        parked = 0;
+        lc[0] = lc[1] = lc[2] = 0;
+        if (exhausted) term = true;
     }
-    if (ANY) return false;
-    return hit->inst >= 0;
+    return found;
 }
 
 // DiffuseAreaQuadLight::intersect_plane (light.rs:86-107).
@@ -278,8 +295,11 @@ __device__ __forceinline__ bool quad_intersect(const DevQuadLight& L, const f3& 
 
 // Closest hit including quad lights (lights after primitives with strict `<`,
 // scene.rs:78-94).
-__device__ __forceinline__ void trace_closest_with_lights(const DevScene& S, const TraceRay& r, TraceHit* hit) {
-    trace_scene<false>(S, r, hit);
+// All lanes of the warp must call it (see trace_warp).
+__device__ __forceinline__ void trace_closest_with_lights(const DevScene& S, const TraceRay& r, bool valid,
+                                                          TraceHit* hit) {
+    trace_warp<false>(S, r, valid, hit);
+    if (!valid) return;
     float best = hit->inst >= 0 ? hit->t : r.tmax;
     for (uint32_t l = 0; l < S.n_lights; ++l) {
         float t; f3 p;

@@ -159,19 +159,24 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, PathSoA P, uint32_t 
         if (lane == 0) base = atomicAdd(fetch, 32u);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n) break;
-        uint32_t j = base + lane;
-        if (j < n) {
-            uint32_t i = depth == 0 ? j : qin[j];
-            float4 ro = P.ray_o[i], rd = P.ray_d[i];
-            TraceRay r;
+        const uint32_t j = base + lane;
+        const bool valid = j < n;
+        const uint32_t i = !valid ? 0u : (depth == 0 ? j : qin[j]);
+        TraceRay r;
+        r.tmin = 1e-4f;
+        r.tmax = __int_as_float(0x7f800000);
+        if (valid) {
+            const float4 ro = P.ray_o[i], rd = P.ray_d[i];
             r.o = mk3(ro.x, ro.y, ro.z);
             r.d = mk3(rd.x, rd.y, rd.z);
-            r.tmin = 1e-4f;
-            r.tmax = __int_as_float(0x7f800000);
             r.time = rd.w;
-            TraceHit h;
-            trace_closest_with_lights(S, r, &h);
-            int32_t code = h.light >= 0 ? -2 - h.light : h.inst;
+        } else {
+            r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.time = 0.0f;
+        }
+        TraceHit h;
+        trace_closest_with_lights(S, r, valid, &h);
+        if (valid) {
+            const int32_t code = h.light >= 0 ? -2 - h.light : h.inst;
             P.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
             P.hit_inst[i] = code;
         }
@@ -188,19 +193,23 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene S, PathSoA P, uint32_t 
         if (lane == 0) base = atomicAdd(fetch, 32u);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n) break;
-        uint32_t j = base + lane;
-        if (j < n) {
-            uint32_t target = P.sq[j];
-            float4 so = P.sh_o[target], sd = P.sh_d[target];
-            TraceRay r;
+        const uint32_t j = base + lane;
+        const bool valid = j < n;
+        const uint32_t target = valid ? P.sq[j] : 0u;
+        TraceRay r;
+        r.tmin = 1e-3f;
+        if (valid) {
+            const float4 so = P.sh_o[target], sd = P.sh_d[target];
             r.o = mk3(so.x, so.y, so.z);
             r.d = mk3(sd.x, sd.y, sd.z);
-            r.tmin = 1e-3f;
             r.tmax = so.w;
             r.time = sd.w;
-            TraceHit h;
-            if (trace_scene<true>(S, r, &h)) P.pend[target] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else {
+            r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.tmax = 0.0f; r.time = 0.0f;
         }
+        TraceHit h;
+        const bool occluded = trace_warp<true>(S, r, valid, &h);
+        if (valid && occluded) P.pend[target] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 }
 
@@ -431,19 +440,25 @@ __global__ void __launch_bounds__(128) k_intersect(DevScene S, const float* __re
         if (lane == 0) base = atomicAdd(counter, 32u);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n) break;
-        uint32_t i = base + lane;
-        if (i >= n) continue;
+        const uint32_t i = base + lane;
+        const bool valid = i < n;
         TraceRay r;
-        r.o = mk3(org[3 * (size_t)i], org[3 * (size_t)i + 1], org[3 * (size_t)i + 2]);
-        r.d = mk3(dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]);
-        r.tmin = tmin[i];
-        r.tmax = tmax[i];
-        r.time = time ? time[i] : 0.0f;
+        if (valid) {
+            r.o = mk3(org[3 * (size_t)i], org[3 * (size_t)i + 1], org[3 * (size_t)i + 2]);
+            r.d = mk3(dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]);
+            r.tmin = tmin[i];
+            r.tmax = tmax[i];
+            r.time = time ? time[i] : 0.0f;
+        } else {
+            r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.tmin = 0.0f; r.tmax = 0.0f; r.time = 0.0f;
+        }
         TraceHit h;
         if (ANY) {
-            occluded[i] = trace_scene<true>(S, r, &h) ? 1 : 0;
+            const bool occ = trace_warp<true>(S, r, valid, &h);
+            if (valid) occluded[i] = occ ? 1 : 0;
         } else {
-            trace_closest_with_lights(S, r, &h);
+            trace_closest_with_lights(S, r, valid, &h);
+            if (!valid) continue;
             if (h.light >= 0) {
                 kind[i] = 2; inst[i] = h.light; tri[i] = -1;
                 tt[i] = h.t; uu[i] = 0.0f; vv[i] = 0.0f;
