@@ -255,6 +255,35 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
                 const pyre_render_params* params, pyre_film* film);
 int pyre_get_render_stats(const pyre_ctx* ctx, pyre_render_stats* out);
 
+/* ------------------------------------------------------------- Batch --- */
+
+/* Uploads n_parts scenes as one device scene (shared arrays, one top-level
+ * BVH and light range per part) for pyre_render_batch. Parts cannot carry an
+ * environment map (PYRE_ERR_UNSUPPORTED). No reference counterpart: the
+ * reference renders one scene per process. */
+int pyre_scene_upload_batch(pyre_ctx* ctx, const pyre_scene_desc* parts, uint32_t n_parts, pyre_scene** out);
+
+/* One view of a batch: the CLI render loop (main.rs:248-286) for scene part
+ * `part`, full image, samples [spp_begin, spp_end). */
+typedef struct pyre_batch_job {
+    uint32_t part;
+    pyre_camera_desc camera;
+    uint32_t width, height;
+    uint32_t spp_begin, spp_end;
+    uint32_t max_depth, min_rr_depth;
+    pyre_film film;
+} pyre_batch_job;
+
+/* Renders every job of the batch through the same wavefront: paths of all
+ * jobs share the stage kernels and queues, in waves planned on the host
+ * (jobs packed in order, each job's samples in sample order, so every film is
+ * bit-identical to pyre_render of that job alone). With params->use_graph
+ * the whole batch is captured once as one CUDA graph and replayed with a
+ * single launch. Uses params->wave_paths (0 = automatic) and use_graph;
+ * the per-job fields of params are ignored. */
+int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const pyre_batch_job* jobs, uint32_t n_jobs,
+                      const pyre_render_params* params);
+
 /* Render without allocating. No counterpart in the reference: this entry
  * point exists for callers that cannot call cudaMalloc while they render,
  * e.g. a host application whose GPU memory belongs to its own allocator, or a

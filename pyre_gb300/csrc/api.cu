@@ -192,7 +192,14 @@ int pyre_scene_destroy(pyre_ctx* ctx, pyre_scene* scene) {
     return PYRE_OK;
 }
 
-int pyre_scene_upload(pyre_ctx* ctx, const pyre_scene_desc* desc, pyre_scene** out) {
+}  // extern "C"
+
+// Uploads `desc` as n_parts independent sub-scenes sharing one device scene:
+// instance i and light l belong to part inst_part[i] / light_part[l] (lights
+// grouped by part, in part order). Each part gets its own top-level BVH and
+// light range, so rays of one part never see another part's geometry.
+static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::vector<uint32_t>& inst_part,
+                        const std::vector<uint32_t>& light_part, uint32_t n_parts, pyre_scene** out) {
     if (!ctx || !desc || !out) return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_upload: NULL argument");
     *out = nullptr;
     cudaSetDevice(ctx->device);
@@ -300,48 +307,52 @@ int pyre_scene_upload(pyre_ctx* ctx, const pyre_scene_desc* desc, pyre_scene** o
         for (uint64_t i = 0; i < 3ull * md.n_triangles; ++i) index.push_back(vbase + md.indices[i]);
     }
 
-    // ---- instances and the top-level BVH over their swept bounds
-    std::vector<uint32_t> live;  // instances with geometry
-    std::vector<Aabb> ibox;
-    std::vector<f3> icent;
-    for (uint32_t i = 0; i < desc->n_instances; ++i) {
-        const pyre_instance_desc& id = desc->instances[i];
-        if (mesh_root[id.mesh] < 0) continue;
-        Aabb base = mesh_box[id.mesh];
-        Aabb w = base;
-        if (id.has_motion) {  // MeshInstance::world_bounds, mesh.rs:95-105
-            f3 o0 = mk3(id.offset_t0[0], id.offset_t0[1], id.offset_t0[2]);
-            f3 o1 = mk3(id.offset_t1[0], id.offset_t1[1], id.offset_t1[2]);
-            w.lo = vmin3(base.lo + o0, base.lo + o1);
-            w.hi = vmax3(base.hi + o0, base.hi + o1);
-        }
-        // The top level is an addition of this library: pad it so its test is
-        // never tighter than the reference's per-instance root test.
-        float mag = std::max({std::fabs(w.lo.x), std::fabs(w.lo.y), std::fabs(w.lo.z), std::fabs(w.hi.x),
-                              std::fabs(w.hi.y), std::fabs(w.hi.z), 1e-3f});
-        if (id.has_motion)
-            for (int k = 0; k < 3; ++k)
-                mag = std::max({mag, std::fabs(id.offset_t0[k]), std::fabs(id.offset_t1[k])});
-        float pad = mag * 1e-5f;
-        w.lo = w.lo - splat3(pad);
-        w.hi = w.hi + splat3(pad);
-        live.push_back(i);
-        ibox.push_back(w);
-        icent.push_back((w.lo + w.hi) * 0.5f);
-    }
-    std::vector<DevInstance> inst(live.size());
-    int32_t tlas_root = -1;
+    // ---- instances and one top-level BVH per part over their swept bounds
+    std::vector<DevInstance> inst;
+    std::vector<int32_t> part_tlas(n_parts, -1);
     sc->slot_of_instance.assign(desc->n_instances, -1);
-    if (!live.empty()) {
+    for (uint32_t part = 0; part < n_parts; ++part) {
+        std::vector<uint32_t> live;  // instances of this part with geometry
+        std::vector<Aabb> ibox;
+        std::vector<f3> icent;
+        for (uint32_t i = 0; i < desc->n_instances; ++i) {
+            if (inst_part[i] != part) continue;
+            const pyre_instance_desc& id = desc->instances[i];
+            if (mesh_root[id.mesh] < 0) continue;
+            Aabb base = mesh_box[id.mesh];
+            Aabb w = base;
+            if (id.has_motion) {  // MeshInstance::world_bounds, mesh.rs:95-105
+                f3 o0 = mk3(id.offset_t0[0], id.offset_t0[1], id.offset_t0[2]);
+                f3 o1 = mk3(id.offset_t1[0], id.offset_t1[1], id.offset_t1[2]);
+                w.lo = vmin3(base.lo + o0, base.lo + o1);
+                w.hi = vmax3(base.hi + o0, base.hi + o1);
+            }
+            // The top level is an addition of this library: pad it so its test is
+            // never tighter than the reference's per-instance root test.
+            float mag = std::max({std::fabs(w.lo.x), std::fabs(w.lo.y), std::fabs(w.lo.z), std::fabs(w.hi.x),
+                                  std::fabs(w.hi.y), std::fabs(w.hi.z), 1e-3f});
+            if (id.has_motion)
+                for (int k = 0; k < 3; ++k)
+                    mag = std::max({mag, std::fabs(id.offset_t0[k]), std::fabs(id.offset_t1[k])});
+            float pad = mag * 1e-5f;
+            w.lo = w.lo - splat3(pad);
+            w.hi = w.hi + splat3(pad);
+            live.push_back(i);
+            ibox.push_back(w);
+            icent.push_back((w.lo + w.hi) * 0.5f);
+        }
+        if (live.empty()) continue;
         std::vector<pyre_bvh2_node> tn;
         std::vector<uint32_t> tp;
         build_bvh2(ibox, icent, tn, tp);
-        tlas_root = (int32_t)nodes.size();
-        collapse_bvh2(tn.data(), (uint32_t)tn.size(), (int32_t)nodes.size(), 0, nodes);
+        const int32_t slot_base = (int32_t)inst.size();
+        part_tlas[part] = (int32_t)nodes.size();
+        collapse_bvh2(tn.data(), (uint32_t)tn.size(), (int32_t)nodes.size(), slot_base, nodes);
+        inst.resize(inst.size() + tp.size());
         for (size_t k = 0; k < tp.size(); ++k) {
             uint32_t i = live[tp[k]];
             const pyre_instance_desc& id = desc->instances[i];
-            DevInstance& I = inst[k];
+            DevInstance& I = inst[slot_base + k];
             std::memset(&I, 0, sizeof I);
             const Aabb& rb = mesh_box[id.mesh];
             I.lo[0] = rb.lo.x; I.lo[1] = rb.lo.y; I.lo[2] = rb.lo.z;
@@ -355,8 +366,16 @@ int pyre_scene_upload(pyre_ctx* ctx, const pyre_scene_desc* desc, pyre_scene** o
             I.index_base = (uint32_t)mesh_index_base[id.mesh];
             I.normal_base = mesh_normal_base[id.mesh];
             I.tri_count = desc->meshes[id.mesh].n_triangles;
-            sc->slot_of_instance[i] = (int32_t)k;
+            sc->slot_of_instance[i] = slot_base + (int32_t)k;
         }
+    }
+    const int32_t tlas_root = part_tlas[0];
+    // per-part light ranges (first, count)
+    std::vector<uint32_t> part_light(2 * n_parts, 0);
+    for (uint32_t l = 0; l < desc->n_lights; ++l) {
+        uint32_t pp = light_part[l];
+        if (part_light[2 * pp + 1] == 0) part_light[2 * pp] = l;
+        part_light[2 * pp + 1] += 1;
     }
 
     // ---- materials and lights
@@ -450,6 +469,18 @@ int pyre_scene_upload(pyre_ctx* ctx, const pyre_scene_desc* desc, pyre_scene** o
     if ((rc = upload(ctx, sc, lights, &d_lights)) != PYRE_OK) return fail(rc);
     D.lights = d_lights;
     D.n_lights = (uint32_t)lights.size();
+    int32_t* d_part_tlas = nullptr;
+    uint32_t* d_part_light = nullptr;
+    if ((rc = upload(ctx, sc, part_tlas, &d_part_tlas)) != PYRE_OK) return fail(rc);
+    if ((rc = upload(ctx, sc, part_light, &d_part_light)) != PYRE_OK) return fail(rc);
+    D.part_tlas = d_part_tlas;
+    D.part_light = d_part_light;
+    D.n_parts = n_parts;
+    sc->n_parts = n_parts;
+    sc->part_tlas = part_tlas;
+    sc->part_light = part_light;
+    sc->part_light_max = 0;
+    for (uint32_t pp = 0; pp < n_parts; ++pp) sc->part_light_max = std::max(sc->part_light_max, part_light[2 * pp + 1]);
     if (desc->env) {
         float4* px = nullptr;
         float *mc = nullptr, *cc = nullptr, *mp = nullptr, *cp = nullptr;
@@ -469,6 +500,54 @@ int pyre_scene_upload(pyre_ctx* ctx, const pyre_scene_desc* desc, pyre_scene** o
     sc->n_nodes = nodes.size();
     *out = sc;
     return PYRE_OK;
+}
+
+extern "C" {
+
+int pyre_scene_upload(pyre_ctx* ctx, const pyre_scene_desc* desc, pyre_scene** out) {
+    if (!desc) return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_upload: NULL argument");
+    std::vector<uint32_t> inst_part(desc->n_instances, 0), light_part(desc->n_lights, 0);
+    return upload_parts(ctx, desc, inst_part, light_part, 1, out);
+}
+
+int pyre_scene_upload_batch(pyre_ctx* ctx, const pyre_scene_desc* descs, uint32_t n_parts, pyre_scene** out) {
+    if (!ctx || !descs || !out || n_parts == 0)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_upload_batch: NULL argument or no parts");
+    std::vector<pyre_mesh_desc> meshes;
+    std::vector<pyre_instance_desc> insts;
+    std::vector<pyre_material_desc> mats;
+    std::vector<pyre_quad_light_desc> lights;
+    std::vector<uint32_t> inst_part, light_part;
+    for (uint32_t p = 0; p < n_parts; ++p) {
+        const pyre_scene_desc& d = descs[p];
+        if (d.env) return set_error(ctx, PYRE_ERR_UNSUPPORTED, "batched scenes cannot carry environment maps");
+        if ((d.n_meshes && !d.meshes) || (d.n_instances && !d.instances) || (d.n_materials && !d.materials) ||
+            (d.n_lights && !d.lights))
+            return set_error(ctx, PYRE_ERR_INVALID, "batch part " + std::to_string(p) + ": NULL array");
+        const uint32_t mesh_base = (uint32_t)meshes.size(), mat_base = (uint32_t)mats.size();
+        meshes.insert(meshes.end(), d.meshes, d.meshes + d.n_meshes);
+        mats.insert(mats.end(), d.materials, d.materials + d.n_materials);
+        for (uint32_t i = 0; i < d.n_instances; ++i) {
+            pyre_instance_desc id = d.instances[i];
+            if (id.mesh >= d.n_meshes || id.material >= d.n_materials)
+                return set_error(ctx, PYRE_ERR_INVALID, "batch part " + std::to_string(p) + ": index out of range");
+            id.mesh += mesh_base;
+            id.material += mat_base;
+            insts.push_back(id);
+            inst_part.push_back(p);
+        }
+        for (uint32_t l = 0; l < d.n_lights; ++l) {
+            lights.push_back(d.lights[l]);
+            light_part.push_back(p);
+        }
+    }
+    pyre_scene_desc merged;
+    std::memset(&merged, 0, sizeof merged);
+    merged.meshes = meshes.data(); merged.n_meshes = (uint32_t)meshes.size();
+    merged.instances = insts.data(); merged.n_instances = (uint32_t)insts.size();
+    merged.materials = mats.data(); merged.n_materials = (uint32_t)mats.size();
+    merged.lights = lights.data(); merged.n_lights = (uint32_t)lights.size();
+    return upload_parts(ctx, &merged, inst_part, light_part, n_parts, out);
 }
 
 int pyre_scene_get_info(const pyre_scene* scene, pyre_scene_info* out) {

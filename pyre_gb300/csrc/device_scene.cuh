@@ -69,6 +69,10 @@ struct DevScene {
     int has_env;
     DevEnv env;
     int* error_flag;       // set to PYRE_ERR_OVERFLOW by a kernel that hit a limit
+    // sub-scenes of a batch upload (one part for an ordinary scene)
+    const int32_t* part_tlas;    // top-level root per part
+    const uint32_t* part_light;  // (first light, light count) per part
+    uint32_t n_parts;
 };
 
 struct TraceRay {
@@ -148,7 +152,8 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 #define PYRE_NODE_EXIT (-2)
 
 template <bool ANY>
-__device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r, bool valid, TraceHit* hit) {
+__device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r, bool valid, int32_t root,
+                                           TraceHit* hit) {
     const unsigned FULL = 0xffffffffu;
     hit->inst = -1; hit->tri = -1; hit->light = -1;
     hit->t = r.tmax; hit->u = 0.0f; hit->v = 0.0f;
@@ -158,11 +163,11 @@ __device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r,
     int32_t best_orig = 0x7fffffff;
     bool found = false;
     // term: the lane has nothing left to do; exhausted: no node left to step
-    bool term = !valid || S.tlas_root < 0;
+    bool term = !valid || root < 0;
     bool exhausted = term;
     int stack[PYRE_STACK];
     int sp = 0;
-    int node = term ? PYRE_NODE_NONE : (S.tlas_root | PYRE_TAG_TOP);
+    int node = term ? PYRE_NODE_NONE : (root | PYRE_TAG_TOP);
     int inst = -1;
     int32_t inst_orig = 0;
     f3 o = r.o;
@@ -296,12 +301,15 @@ __device__ __forceinline__ bool quad_intersect(const DevQuadLight& L, const f3& 
 // Closest hit including quad lights (lights after primitives with strict `<`,
 // scene.rs:78-94).
 // All lanes of the warp must call it (see trace_warp).
+// `root` is the top-level BVH to trace (S.tlas_root, or a batch part's) and
+// [light_first, light_first + light_count) the quad lights it can hit.
 __device__ __forceinline__ void trace_closest_with_lights(const DevScene& S, const TraceRay& r, bool valid,
+                                                          int32_t root, uint32_t light_first, uint32_t light_count,
                                                           TraceHit* hit) {
-    trace_warp<false>(S, r, valid, hit);
+    trace_warp<false>(S, r, valid, root, hit);
     if (!valid) return;
     float best = hit->inst >= 0 ? hit->t : r.tmax;
-    for (uint32_t l = 0; l < S.n_lights; ++l) {
+    for (uint32_t l = light_first; l < light_first + light_count; ++l) {
         float t; f3 p;
         if (quad_intersect(S.lights[l], r.o, r.d, r.tmin, best, &t, &p) && t < best) {
             best = t;

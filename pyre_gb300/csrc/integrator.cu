@@ -43,6 +43,27 @@ struct WaveCtl {
     unsigned long long extend_rays, shadow_rays, samples;
 };
 
+// Batched rendering: per-job view, per-wave segments (a segment = one job's
+// consecutive samples s_first .. s_first+s_count-1 over all its pixels).
+struct DevJob {
+    DevCamera cam;
+    uint32_t width, height, npix;
+    uint32_t spp_begin, spp_end, max_depth, min_rr;
+    int32_t tlas_root;
+    uint32_t light_first, light_count;
+    uint32_t acc_base;  // first film accumulator of the job
+    float inv_spp;
+};
+struct DevSeg {
+    uint32_t job, s_first, s_count;
+    uint32_t path_base;  // first path of the segment in the wave
+    uint32_t slot_base;  // first accumulate slot (one per pixel) of the segment
+};
+struct DevWave {
+    uint32_t seg_first, seg_count;
+    uint32_t n_paths, n_slots;
+};
+
 struct WaveParams {
     DevCamera cam;
     uint32_t width, height;
@@ -51,6 +72,10 @@ struct WaveParams {
     uint32_t max_depth, min_rr;
     uint32_t ns;  // NEE slots per path: lights (+1 for the environment)
     int env_cdf;
+    // batch tables (null for a single view)
+    const DevJob* jobs;
+    const DevSeg* segs;
+    const DevWave* waves;
 };
 
 struct PathSoA {
@@ -72,6 +97,7 @@ struct PathSoA {
     float4* acc_a;     // albedo sum
     float4* acc_n;     // normal sum
     WaveCtl* ctl;
+    uint32_t* pjob;    // batch: job of each path
 };
 
 __device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
@@ -110,6 +136,30 @@ __global__ void k_wave_begin(WaveCtl* ctl, uint32_t spp_begin, uint32_t spp_end,
     ctl->count[0] = k_valid * npix;
 }
 
+__global__ void k_wave_begin_batch(WaveCtl* ctl, const DevWave* waves) {
+    if (threadIdx.x != 0) return;
+    const DevWave w = waves[ctl->wave];
+    ctl->s_base = 0;
+    ctl->k_valid = 0;
+    ctl->n_valid = w.n_paths;
+    for (int d = 0; d <= PYRE_MAX_DEPTH; ++d) ctl->count[d] = 0;
+    for (int d = 0; d < PYRE_MAX_DEPTH; ++d) ctl->scount[d] = 0;
+    for (int d = 0; d < 2 * PYRE_MAX_DEPTH; ++d) ctl->fetch[d] = 0;
+    ctl->count[0] = w.n_paths;
+}
+
+// Segment of the current wave holding path (or slot) i: last segment whose
+// base is <= i (binary search over the wave's segments).
+__device__ __forceinline__ uint32_t find_segment(const DevSeg* segs, const DevWave& w, uint32_t i, bool by_slot) {
+    uint32_t lo = w.seg_first, hi = w.seg_first + w.seg_count - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) / 2;
+        uint32_t b = by_slot ? segs[mid].slot_base : segs[mid].path_base;
+        if (b <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
 __global__ void k_wave_end(WaveCtl* ctl, uint32_t max_depth) {
     if (threadIdx.x != 0) return;
     unsigned long long e = 0, s = 0;
@@ -121,22 +171,37 @@ __global__ void k_wave_end(WaveCtl* ctl, uint32_t max_depth) {
 }
 
 // main.rs:261-273: seed, jitter, ndc, lens, time, Camera::generate_ray.
+template <bool BATCH>
 __global__ void k_raygen(PathSoA P, WaveParams W) {
     const uint32_t n = P.ctl->n_valid;
     const uint32_t s_base = P.ctl->s_base;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t k = i / W.npix, p = i - k * W.npix;
-        uint32_t x = W.cx0 + p % W.cw, y = W.cy0 + p / W.cw;
+        uint32_t x, y, s, width, height;
+        const DevCamera* cam = &W.cam;
+        if (BATCH) {
+            const DevWave& wv = W.waves[P.ctl->wave];
+            const DevSeg sg = W.segs[find_segment(W.segs, wv, i, false)];
+            const DevJob& J = W.jobs[sg.job];
+            const uint32_t local = i - sg.path_base, k = local / J.npix, p = local - k * J.npix;
+            x = p % J.width; y = p / J.width; s = sg.s_first + k;
+            width = J.width; height = J.height;
+            cam = &J.cam;
+            P.pjob[i] = sg.job;
+        } else {
+            const uint32_t k = i / W.npix, p = i - k * W.npix;
+            x = W.cx0 + p % W.cw; y = W.cy0 + p / W.cw; s = s_base + k;
+            width = W.width; height = W.height;
+        }
         Rng g;
-        g.seed(pixel_seed(x, y, s_base + k));
+        g.seed(pixel_seed(x, y, s));
         float jx = g.next_f32(), jy = g.next_f32();
         f2 ndc;
-        ndc.x = 2.0f * ((float)x + jx) / (float)W.width - 1.0f;
-        ndc.y = 1.0f - 2.0f * ((float)y + jy) / (float)W.height;
+        ndc.x = 2.0f * ((float)x + jx) / (float)width - 1.0f;
+        ndc.y = 1.0f - 2.0f * ((float)y + jy) / (float)height;
         f2 lens = g.next_vec2();
         float time = g.next_f32();
         f3 o, d;
-        camera_ray(W.cam, ndc, lens, &o, &d);
+        camera_ray(*cam, ndc, lens, &o, &d);
         P.ray_o[i] = make_float4(o.x, o.y, o.z, 1e-4f);
         P.ray_d[i] = make_float4(d.x, d.y, d.z, time);
         store_rng(P.rng, i, g);
@@ -149,7 +214,8 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
 }
 
 // ---------------------------------------------------------------- extend --
-__global__ void __launch_bounds__(128) k_extend(DevScene S, PathSoA P, uint32_t depth) {
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     const uint32_t n = P.ctl->count[depth];
     const uint32_t* qin = P.q[depth & 1];
     uint32_t* fetch = &P.ctl->fetch[2 * depth];
@@ -173,8 +239,14 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, PathSoA P, uint32_t 
         } else {
             r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.time = 0.0f;
         }
+        int32_t root = S.tlas_root;
+        uint32_t lfirst = 0, lcount = S.n_lights;
+        if (BATCH && valid) {
+            const DevJob& J = W.jobs[P.pjob[i]];
+            root = J.tlas_root; lfirst = J.light_first; lcount = J.light_count;
+        }
         TraceHit h;
-        trace_closest_with_lights(S, r, valid, &h);
+        trace_closest_with_lights(S, r, valid, root, lfirst, lcount, &h);
         if (valid) {
             const int32_t code = h.light >= 0 ? -2 - h.light : h.inst;
             P.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
@@ -184,7 +256,8 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, PathSoA P, uint32_t 
 }
 
 // ---------------------------------------------------------------- shadow --
-__global__ void __launch_bounds__(128) k_shadow(DevScene S, PathSoA P, uint32_t depth) {
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_shadow(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     const uint32_t n = P.ctl->scount[depth];
     uint32_t* fetch = &P.ctl->fetch[2 * depth + 1];
     const int lane = threadIdx.x & 31;
@@ -207,14 +280,17 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene S, PathSoA P, uint32_t 
         } else {
             r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.tmax = 0.0f; r.time = 0.0f;
         }
+        int32_t root = S.tlas_root;
+        if (BATCH && valid) root = W.jobs[P.pjob[target / W.ns]].tlas_root;
         TraceHit h;
-        const bool occluded = trace_warp<true>(S, r, valid, &h);
+        const bool occluded = trace_warp<true>(S, r, valid, root, &h);
         if (valid && occluded) P.pend[target] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 }
 
 // ----------------------------------------------------------------- shade --
 // One path vertex of PathIntegrator::integrate (integrator.rs:242-388).
+template <bool BATCH>
 __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     const uint32_t n = P.ctl->count[depth];
     const uint32_t* qin = P.q[depth & 1];
@@ -310,10 +386,15 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
             if (wo.z > 0.0f) {
                 Rng g = load_rng(P.rng, i);
                 const f3 p_off = p + 1e-3f * ns;
+                uint32_t lfirst = 0, lcount = S.n_lights;
+                if (BATCH) {
+                    const DevJob& J = W.jobs[P.pjob[i]];
+                    lfirst = J.light_first; lcount = J.light_count;
+                }
                 // NEE over every quad light (integrator.rs:307-333).
-                for (uint32_t l = 0; l < S.n_lights; ++l) {
+                for (uint32_t l = 0; l < lcount; ++l) {
                     f2 ul = g.next_vec2();
-                    const DevQuadLight& Lt = S.lights[l];
+                    const DevQuadLight& Lt = S.lights[lfirst + l];
                     f3 lpos, lwi;
                     float lpdf;
                     if (!quad_sample(Lt, p, ul, &lpos, &lwi, &lpdf)) continue;
@@ -369,7 +450,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
                     if (cos_wi != 0.0f) {
                         beta = beta * (bf * cos_wi / bpdf);
                         bool survive = true;
-                        if (depth >= W.min_rr) {
+                        if (depth >= (BATCH ? W.jobs[P.pjob[i]].min_rr : W.min_rr)) {
                             float q = clampf_(1.0f - max_elem3(beta), 0.05f, 0.95f);
                             if (g.next_f32() < q) survive = false;
                             else beta = beta / (1.0f - q);
@@ -388,7 +469,8 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
             }
         }
         P.L[i] = make_float4(L.x, L.y, L.z, 0.0f);
-        if (alive && depth + 1 < W.max_depth) qout[append_slot(next_count)] = i;
+        if (alive && depth + 1 < (BATCH ? W.jobs[P.pjob[i]].max_depth : W.max_depth))
+            qout[append_slot(next_count)] = i;
     }
 }
 
@@ -413,6 +495,54 @@ __global__ void k_accumulate(PathSoA P, WaveParams W) {
             an.x += nn.x; an.y += nn.y; an.z += nn.z;
         }
         P.acc_r[p] = ar; P.acc_a[p] = aa; P.acc_n[p] = an;
+    }
+}
+
+// Batch: one thread per (segment, pixel) slot of the wave; samples of the
+// segment are added in sample order into the job's accumulators.
+__global__ void k_accumulate_batch(PathSoA P, WaveParams W) {
+    const DevWave wv = W.waves[P.ctl->wave];
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < wv.n_slots; q += gridDim.x * blockDim.x) {
+        const DevSeg sg = W.segs[find_segment(W.segs, wv, q, true)];
+        const DevJob& J = W.jobs[sg.job];
+        const uint32_t p = q - sg.slot_base;
+        const uint32_t a = J.acc_base + p;
+        float4 ar = P.acc_r[a], aa = P.acc_a[a], an = P.acc_n[a];
+        for (uint32_t k = 0; k < sg.s_count; ++k) {
+            const uint32_t i = sg.path_base + k * J.npix + p;
+            float4 Lq = P.L[i];
+            f3 L = mk3(Lq.x, Lq.y, Lq.z);
+            for (uint32_t s = 0; s < W.ns; ++s) {
+                float4 c = P.pend[(size_t)i * W.ns + s];
+                if (c.w != 0.0f) L = L + mk3(c.x, c.y, c.z);
+            }
+            float4 al = P.aov_a[i], nn = P.aov_n[i];
+            ar.x += L.x; ar.y += L.y; ar.z += L.z; ar.w += al.w;
+            aa.x += al.x; aa.y += al.y; aa.z += al.z;
+            an.x += nn.x; an.y += nn.y; an.z += nn.z;
+        }
+        P.acc_r[a] = ar; P.acc_a[a] = aa; P.acc_n[a] = an;
+    }
+}
+
+// Batch: per-job means into a staging film laid out like the accumulators.
+__global__ void k_finalize_batch(PathSoA P, const DevJob* jobs, uint32_t n_jobs, uint32_t total, float* out) {
+    for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < total; a += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = n_jobs - 1;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi + 1) / 2;
+            if (jobs[mid].acc_base <= a) lo = mid; else hi = mid - 1;
+        }
+        const float inv = jobs[lo].inv_spp;
+        float4 ar = P.acc_r[a], aa = P.acc_a[a], an = P.acc_n[a];
+        float* rad = out;
+        float* alb = out + 3 * (size_t)total;
+        float* nor = out + 6 * (size_t)total;
+        float* dep = out + 9 * (size_t)total;
+        rad[3 * (size_t)a] = ar.x * inv; rad[3 * (size_t)a + 1] = ar.y * inv; rad[3 * (size_t)a + 2] = ar.z * inv;
+        alb[3 * (size_t)a] = aa.x * inv; alb[3 * (size_t)a + 1] = aa.y * inv; alb[3 * (size_t)a + 2] = aa.z * inv;
+        nor[3 * (size_t)a] = an.x * inv; nor[3 * (size_t)a + 1] = an.y * inv; nor[3 * (size_t)a + 2] = an.z * inv;
+        dep[a] = ar.w * inv;
     }
 }
 
@@ -454,10 +584,10 @@ __global__ void __launch_bounds__(128) k_intersect(DevScene S, const float* __re
         }
         TraceHit h;
         if (ANY) {
-            const bool occ = trace_warp<true>(S, r, valid, &h);
+            const bool occ = trace_warp<true>(S, r, valid, S.tlas_root, &h);
             if (valid) occluded[i] = occ ? 1 : 0;
         } else {
-            trace_closest_with_lights(S, r, valid, &h);
+            trace_closest_with_lights(S, r, valid, S.tlas_root, 0, S.n_lights, &h);
             if (!valid) continue;
             if (h.light >= 0) {
                 kind[i] = 2; inst[i] = h.light; tri[i] = -1;
@@ -498,7 +628,7 @@ struct Carver {
     }
 };
 
-size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* out) {
+size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* out, bool batch = false) {
     Carver c{base};
     PathSoA s;
     s.ray_o = c.take<float4>(P);
@@ -520,6 +650,7 @@ size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* ou
     s.acc_a = c.take<float4>(npix);
     s.acc_n = c.take<float4>(npix);
     s.ctl = c.take<WaveCtl>(1);
+    s.pjob = batch ? c.take<uint32_t>(P) : nullptr;
     if (out) *out = s;
     return c.off + 256;
 }
@@ -568,19 +699,42 @@ void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Wave
     cudaStream_t st = ctx->stream;
     mark(ctx, STAGE_OTHER);
     k_wave_begin<<<1, 32, 0, st>>>(P.ctl, W.spp_begin, W.spp_end, W.k_per_wave, W.npix);
-    k_raygen<<<Lc.grid_raygen, 256, 0, st>>>(P, W);
+    k_raygen<false><<<Lc.grid_raygen, 256, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
-        k_extend<<<Lc.grid_extend, 128, 0, st>>>(S, P, d);
+        k_extend<false><<<Lc.grid_extend, 128, 0, st>>>(S, P, W, d);
         mark(ctx, STAGE_SHADE);
-        k_shade<<<Lc.grid_shade, 256, 0, st>>>(S, P, W, d);
+        k_shade<false><<<Lc.grid_shade, 256, 0, st>>>(S, P, W, d);
         if (W.ns > 0) {
             mark(ctx, STAGE_SHADOW);
-            k_shadow<<<Lc.grid_shadow, 128, 0, st>>>(S, P, d);
+            k_shadow<false><<<Lc.grid_shadow, 128, 0, st>>>(S, P, W, d);
         }
     }
     mark(ctx, STAGE_OTHER);
     k_accumulate<<<Lc.grid_acc, 256, 0, st>>>(P, W);
+    k_wave_end<<<1, 32, 0, st>>>(P.ctl, W.max_depth);
+    mark(ctx, STAGE_END);
+}
+
+// One batch wave: the same stages over paths of several jobs; W.max_depth is
+// the deepest job's (shallower jobs stop enqueueing their paths earlier).
+void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const WaveParams& W, const Launch& Lc) {
+    cudaStream_t st = ctx->stream;
+    mark(ctx, STAGE_OTHER);
+    k_wave_begin_batch<<<1, 32, 0, st>>>(P.ctl, W.waves);
+    k_raygen<true><<<Lc.grid_raygen, 256, 0, st>>>(P, W);
+    for (uint32_t d = 0; d < W.max_depth; ++d) {
+        mark(ctx, STAGE_EXTEND);
+        k_extend<true><<<Lc.grid_extend, 128, 0, st>>>(S, P, W, d);
+        mark(ctx, STAGE_SHADE);
+        k_shade<true><<<Lc.grid_shade, 256, 0, st>>>(S, P, W, d);
+        if (W.ns > 0) {
+            mark(ctx, STAGE_SHADOW);
+            k_shadow<true><<<Lc.grid_shadow, 128, 0, st>>>(S, P, W, d);
+        }
+    }
+    mark(ctx, STAGE_OTHER);
+    k_accumulate_batch<<<Lc.grid_acc, 256, 0, st>>>(P, W);
     k_wave_end<<<1, 32, 0, st>>>(P.ctl, W.max_depth);
     mark(ctx, STAGE_END);
 }
@@ -639,10 +793,10 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
     if (film->mem == PYRE_MEM_HOST && (rc = ensure_workspace(ctx, ctx->io_ws, film_bytes))) return rc;
 
     Launch Lc;
-    Lc.grid_raygen = grid_for(ctx, k_raygen, 256);
-    Lc.grid_shade = grid_for(ctx, k_shade, 256);
-    Lc.grid_extend = grid_for(ctx, k_extend, 128);
-    Lc.grid_shadow = grid_for(ctx, k_shadow, 128);
+    Lc.grid_raygen = grid_for(ctx, k_raygen<false>, 256);
+    Lc.grid_shade = grid_for(ctx, k_shade<false>, 256);
+    Lc.grid_extend = grid_for(ctx, k_extend<false>, 128);
+    Lc.grid_shadow = grid_for(ctx, k_shadow<false>, 128);
     Lc.grid_acc = grid_for(ctx, k_accumulate, 256);
 
     cudaStream_t st = ctx->stream;
@@ -726,6 +880,172 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
 
 }  // extern "C"
 
+// ----------------------------------------------------------- batch render --
+extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const pyre_batch_job* jobs,
+                                 uint32_t n_jobs, const pyre_render_params* params) {
+    if (!ctx || !scene || !jobs || n_jobs == 0)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_batch: NULL argument or no jobs");
+    PYRE_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    if (scene->dev.has_env)
+        return set_error(ctx, PYRE_ERR_UNSUPPORTED, "pyre_render_batch: environment maps are not batched");
+    const uint32_t wave_paths = params ? params->wave_paths : 0u;
+    const bool use_graph = params && params->use_graph && !ctx->stage_timing;
+
+    // ---- job table
+    std::vector<DevJob> dj(n_jobs);
+    uint64_t total_pix = 0, total_samples = 0, max_npix = 0;
+    uint32_t max_depth = 0;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        const pyre_batch_job& jb = jobs[j];
+        const std::string tag = "batch job " + std::to_string(j) + ": ";
+        if (jb.part >= scene->n_parts) return set_error(ctx, PYRE_ERR_INVALID, tag + "scene part out of range");
+        if (jb.width == 0 || jb.height == 0) return set_error(ctx, PYRE_ERR_INVALID, tag + "image size is zero");
+        if (jb.spp_end <= jb.spp_begin) return set_error(ctx, PYRE_ERR_INVALID, tag + "empty sample range");
+        if (jb.max_depth > PYRE_MAX_DEPTH) return set_error(ctx, PYRE_ERR_INVALID, tag + "max_depth above 64");
+        if (jb.camera.kind > PYRE_CAMERA_THIN_LENS) return set_error(ctx, PYRE_ERR_INVALID, tag + "bad camera");
+        if (jb.film.mem != PYRE_MEM_HOST && jb.film.mem != PYRE_MEM_DEVICE)
+            return set_error(ctx, PYRE_ERR_INVALID, tag + "bad film.mem");
+        DevJob& d = dj[j];
+        std::memset(&d, 0, sizeof d);
+        d.cam = make_camera(jb.camera);
+        d.width = jb.width; d.height = jb.height;
+        d.npix = jb.width * jb.height;
+        d.spp_begin = jb.spp_begin; d.spp_end = jb.spp_end;
+        d.max_depth = jb.max_depth; d.min_rr = jb.min_rr_depth;
+        d.tlas_root = scene->part_tlas[jb.part];
+        d.light_first = scene->part_light[2 * jb.part];
+        d.light_count = scene->part_light[2 * jb.part + 1];
+        d.acc_base = (uint32_t)total_pix;
+        d.inv_spp = 1.0f / (float)(jb.spp_end - jb.spp_begin);
+        total_pix += d.npix;
+        total_samples += (uint64_t)d.npix * (jb.spp_end - jb.spp_begin);
+        max_npix = std::max<uint64_t>(max_npix, d.npix);
+        max_depth = std::max(max_depth, jb.max_depth);
+    }
+    if (total_pix > 0x7fffffffull) return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_batch: too many pixels");
+
+    // ---- wave plan: jobs packed in order, each job's samples in order
+    uint64_t cap = wave_paths ? wave_paths : (uint64_t)8 << 20;
+    cap = std::min<uint64_t>(std::max<uint64_t>(cap, max_npix), (uint64_t)1 << 31);
+    std::vector<DevSeg> segs;
+    std::vector<DevWave> waves;
+    DevWave cur{0, 0, 0, 0};
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        uint32_t s = jobs[j].spp_begin, remaining = jobs[j].spp_end - jobs[j].spp_begin;
+        while (remaining > 0) {
+            uint64_t k = std::min<uint64_t>(remaining, (cap - cur.n_paths) / dj[j].npix);
+            if (k == 0) {
+                waves.push_back(cur);
+                cur = DevWave{(uint32_t)segs.size(), 0, 0, 0};
+                continue;
+            }
+            segs.push_back(DevSeg{j, s, (uint32_t)k, cur.n_paths, cur.n_slots});
+            cur.seg_count += 1;
+            cur.n_paths += (uint32_t)(k * dj[j].npix);
+            cur.n_slots += dj[j].npix;
+            s += (uint32_t)k;
+            remaining -= (uint32_t)k;
+        }
+    }
+    if (cur.seg_count) waves.push_back(cur);
+    uint64_t max_paths = 0;
+    for (const DevWave& w : waves) max_paths = std::max<uint64_t>(max_paths, w.n_paths);
+
+    WaveParams W;
+    std::memset(&W, 0, sizeof W);
+    W.max_depth = max_depth;
+    W.ns = scene->part_light_max;
+    const uint32_t ns = std::max(W.ns, 1u);
+
+    // ---- workspace: path state, accumulators, tables, staging film
+    const size_t path_bytes = carve_paths(nullptr, max_paths, ns, (uint32_t)total_pix, nullptr, true);
+    const size_t job_bytes = dj.size() * sizeof(DevJob), seg_bytes = segs.size() * sizeof(DevSeg),
+                 wave_bytes = waves.size() * sizeof(DevWave);
+    const size_t stage_bytes = total_pix * 10 * sizeof(float);
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t need = al(path_bytes) + al(job_bytes) + al(seg_bytes) + al(wave_bytes) + al(stage_bytes);
+    int rc = ensure_workspace(ctx, ctx->render_ws, need);
+    if (rc) return rc;
+    char* base = (char*)ctx->render_ws.ptr;
+    PathSoA S;
+    carve_paths(base, max_paths, ns, (uint32_t)total_pix, &S, true);
+    DevJob* d_jobs = (DevJob*)(base + al(path_bytes));
+    DevSeg* d_segs = (DevSeg*)((char*)d_jobs + al(job_bytes));
+    DevWave* d_waves = (DevWave*)((char*)d_segs + al(seg_bytes));
+    float* d_stage = (float*)((char*)d_waves + al(wave_bytes));
+    W.jobs = d_jobs; W.segs = d_segs; W.waves = d_waves;
+
+    cudaStream_t st = ctx->stream;
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(d_jobs, dj.data(), job_bytes, cudaMemcpyHostToDevice, st));
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(d_segs, segs.data(), seg_bytes, cudaMemcpyHostToDevice, st));
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(d_waves, waves.data(), wave_bytes, cudaMemcpyHostToDevice, st));
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_r, 0, total_pix * sizeof(float4), st));
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_a, 0, total_pix * sizeof(float4), st));
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_n, 0, total_pix * sizeof(float4), st));
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
+
+    Launch Lc;
+    Lc.grid_raygen = grid_for(ctx, k_raygen<true>, 256);
+    Lc.grid_shade = grid_for(ctx, k_shade<true>, 256);
+    Lc.grid_extend = grid_for(ctx, k_extend<true>, 128);
+    Lc.grid_shadow = grid_for(ctx, k_shadow<true>, 128);
+    Lc.grid_acc = grid_for(ctx, k_accumulate_batch, 256);
+
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
+    ctx->stage_used = 0;
+    const uint32_t n_waves = (uint32_t)waves.size();
+    if (use_graph) {
+        // The whole batch (every wave) as one graph, launched once.
+        std::string key = "batch/" + std::to_string(scene->serial) + "/" +
+                          std::to_string((uintptr_t)ctx->render_ws.ptr) + "/" + std::to_string(n_waves) + "/" +
+                          std::to_string(max_depth) + "/" + std::to_string(max_paths) + "/";
+        key.append(reinterpret_cast<const char*>(dj.data()), job_bytes);
+        if (!ctx->wave_graph || ctx->wave_graph_key != key) {
+            if (ctx->wave_graph) { cudaGraphExecDestroy(ctx->wave_graph); ctx->wave_graph = nullptr; }
+            cudaGraph_t g;
+            PYRE_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            for (uint32_t w = 0; w < n_waves; ++w) enqueue_wave_batch(ctx, scene->dev, S, W, Lc);
+            PYRE_CUDA_TRY(ctx, cudaStreamEndCapture(st, &g));
+            cudaError_t e = cudaGraphInstantiate(&ctx->wave_graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { ctx->wave_graph = nullptr; return cuda_check(ctx, e, "cudaGraphInstantiate"); }
+            ctx->wave_graph_key = key;
+        }
+        PYRE_CUDA_TRY(ctx, cudaGraphLaunch(ctx->wave_graph, st));
+    } else {
+        for (uint32_t w = 0; w < n_waves; ++w) enqueue_wave_batch(ctx, scene->dev, S, W, Lc);
+    }
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    k_finalize_batch<<<Lc.grid_acc, 256, 0, st>>>(S, d_jobs, n_jobs, (uint32_t)total_pix, d_stage);
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[1], st));
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        const pyre_film& f = jobs[j].film;
+        const cudaMemcpyKind kind = f.mem == PYRE_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+        const size_t a = dj[j].acc_base, n = dj[j].npix;
+        float* outs[4] = {f.radiance, f.albedo, f.normal, f.depth};
+        for (int c = 0; c < 4; ++c) {
+            if (!outs[c]) continue;
+            const size_t comps = c == 3 ? 1 : 3;
+            const float* src = d_stage + (size_t)c * 3 * total_pix + comps * a;
+            PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(outs[c], src, comps * n * sizeof(float), kind, st));
+        }
+    }
+    WaveCtl ctl;
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(&ctl, S.ctl, sizeof ctl, cudaMemcpyDeviceToHost, st));
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    if ((rc = take_kernel_error(ctx))) return rc;
+    pyre_render_stats& s = ctx->stats;
+    std::memset(&s, 0, sizeof s);
+    s.samples = ctl.samples;
+    s.extend_rays = ctl.extend_rays;
+    s.shadow_rays = ctl.shadow_rays;
+    s.waves = n_waves;
+    s.kernel_launches = n_waves * kernels_per_wave(W) + 1;
+    cudaEventElapsedTime(&s.ms_total, ctx->ev[0], ctx->ev[1]);
+    return PYRE_OK;
+}
+
 // --------------------------------------------------- render without malloc --
 // Path state for pyre_render_noalloc: one static array per device that loads
 // the library, used in place of the context's cudaMalloc'd workspace.
@@ -808,10 +1128,10 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     carve_paths((char*)scratch, (size_t)W.npix * K, ns, W.npix, &S);
 
     Launch Lc;
-    Lc.grid_raygen = grid_for(ctx, k_raygen, 256);
-    Lc.grid_shade = grid_for(ctx, k_shade, 256);
-    Lc.grid_extend = grid_for(ctx, k_extend, 128);
-    Lc.grid_shadow = grid_for(ctx, k_shadow, 128);
+    Lc.grid_raygen = grid_for(ctx, k_raygen<false>, 256);
+    Lc.grid_shade = grid_for(ctx, k_shade<false>, 256);
+    Lc.grid_extend = grid_for(ctx, k_extend<false>, 128);
+    Lc.grid_shadow = grid_for(ctx, k_shadow<false>, 128);
     Lc.grid_acc = grid_for(ctx, k_accumulate, 256);
 
     cudaStream_t st = ctx->stream;

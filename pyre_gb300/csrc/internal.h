@@ -13,6 +13,10 @@ struct pyre_scene {
     std::vector<int32_t> slot_of_instance;  // original instance id -> device slot
     uint32_t n_triangles = 0;
     uint64_t n_nodes = 0;
+    uint32_t n_parts = 1;         // sub-scenes (pyre_scene_upload_batch)
+    uint32_t part_light_max = 0;  // most quad lights in one part
+    std::vector<int32_t> part_tlas;    // host copies of the per-part tables
+    std::vector<uint32_t> part_light;  // (first, count) per part
     uint64_t device_bytes = 0;
 };
 

@@ -103,6 +103,12 @@ class Film(C.Structure):
     _fields_ = [("radiance", P_f), ("albedo", P_f), ("normal", P_f), ("depth", P_f), ("mem", C.c_int)]
 
 
+class BatchJob(C.Structure):
+    _fields_ = [("part", C.c_uint32), ("camera", CameraDesc), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("spp_begin", C.c_uint32), ("spp_end", C.c_uint32), ("max_depth", C.c_uint32),
+                ("min_rr_depth", C.c_uint32), ("film", Film)]
+
+
 class SceneInfo(C.Structure):
     _fields_ = [("n_triangles", C.c_uint64), ("n_nodes", C.c_uint64), ("n_instances", C.c_uint64),
                 ("triangle_bytes", C.c_uint64), ("node_bytes", C.c_uint64), ("device_bytes", C.c_uint64)]
@@ -132,6 +138,9 @@ SIGNATURES = {
     "pyre_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams),
                                       C.POINTER(Film)]),
     "pyre_set_stage_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "pyre_scene_upload_batch": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.c_uint32, C.POINTER(C.c_void_p)]),
+    "pyre_render_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(BatchJob), C.c_uint32,
+                                    C.POINTER(RenderParams)]),
 }
 
 

@@ -375,3 +375,30 @@ def studio_procedural_camera(width: int = 1920, height: int = 1080, aperture: fl
 
 
 DEFAULT_INTEGRATOR = PathIntegrator(8, 3)
+
+
+# ------------------------------------------------------------ batch jobs --
+def batch_jobs(n_jobs: int = 256, seed: int = 11, resolutions=(128, 256, 512, 1024), spps=(4, 16, 64),
+               depth_range=(4, 12), tri_range=(10, 200_000)):
+    """Batched-rendering workload: Cornell-box variants, each with a seeded
+    displaced-sphere insert of log-uniform triangle count, a seeded Disney
+    material on it, a random square resolution, spp and max depth.
+
+    Returns a list of dicts: scene, camera, width, height, spp, integrator.
+    """
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for j in range(n_jobs):
+        sc = cornell_box()
+        n_tri = float(np.exp(rng.uniform(np.log(tri_range[0]), np.log(tri_range[1]))))
+        seg = max(3, int(round((n_tri / 2.0) ** 0.5)))  # a seg x seg UV grid has 2*seg^2 triangles
+        center = (rng.uniform(-0.4, 0.4), -0.55, rng.uniform(-0.3, 0.5))
+        mesh = displaced_sphere(center, 0.3, seg, seed=5000 + j, amplitude=0.08)
+        sc.materials.append(DisneyBsdf(rng.random(3), 1.0 if rng.random() < 0.3 else 0.0,
+                                       0.05 + 0.95 * rng.random(), 0.5))
+        sc.primitives.append(Primitive(MeshInstance.build(mesh), len(sc.materials) - 1))
+        res = int(rng.choice(resolutions))
+        jobs.append({"scene": sc, "camera": cornell_box_camera(res, res), "width": res, "height": res,
+                     "spp": int(rng.choice(spps)),
+                     "integrator": PathIntegrator(int(rng.integers(depth_range[0], depth_range[1] + 1)), 3)})
+    return jobs

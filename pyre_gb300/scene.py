@@ -385,6 +385,38 @@ class CudaIntegrator:
         self.check(self.lib.pyre_render(self.handle, dscene.handle, C.byref(cam), C.byref(p), C.byref(f)))
         return film
 
+    def upload_batch(self, scenes: list) -> DeviceScene:
+        """pyre_scene_upload_batch: one device scene with one part per scene."""
+        flats = [_Flat(s) for s in scenes]
+        arr = (N.SceneDesc * len(flats))(*[f.desc for f in flats])
+        h = C.c_void_p()
+        self.check(self.lib.pyre_scene_upload_batch(self.handle, arr, len(flats), C.byref(h)))
+        return DeviceScene(self, h, scenes)
+
+    def render_batch(self, dscene: DeviceScene, jobs: list, wave_paths: int = 0, use_graph: int = 0) -> list:
+        """jobs: dicts with part, camera, width, height, spp, spp_begin (0), integrator -> list of Films."""
+        films, cjobs = [], []
+        for jb in jobs:
+            w, h = jb["width"], jb["height"]
+            film = Film(w, h)
+            films.append(film)
+            it = jb.get("integrator", PathIntegrator())
+            b = N.BatchJob()
+            b.part = jb["part"]
+            b.camera = jb["camera"].to_desc()
+            b.width, b.height = w, h
+            b.spp_begin = jb.get("spp_begin", 0)
+            b.spp_end = b.spp_begin + jb["spp"]
+            b.max_depth, b.min_rr_depth = it.max_depth, it.min_rr_depth
+            b.film = N.Film(N.fptr(film.radiance), N.fptr(film.albedo), N.fptr(film.normal), N.fptr(film.depth),
+                            N.PYRE_MEM_HOST)
+            cjobs.append(b)
+        arr = (N.BatchJob * len(cjobs))(*cjobs)
+        p = N.RenderParams()
+        p.wave_paths, p.use_graph = wave_paths, use_graph
+        self.check(self.lib.pyre_render_batch(self.handle, dscene.handle, arr, len(cjobs), C.byref(p)))
+        return films
+
     def render_into(self, dscene: DeviceScene, camera: CameraSpec, params: N.RenderParams, film: N.Film) -> None:
         """pyre_render into caller-provided film buffers (host or device pointers)."""
         cam = camera.to_desc()
