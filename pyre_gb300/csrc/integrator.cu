@@ -675,9 +675,29 @@ DevCamera make_camera(const pyre_camera_desc& c) {
 }
 
 struct Launch {
-    int block_stage = 256;
+    int block_shade = 256;  // raygen, shade, accumulate (at most 256)
+    int block_trace = 128;  // extend, shadow (at most 128)
     int grid_raygen, grid_shade, grid_extend, grid_shadow, grid_acc;
 };
+
+// Grid sizes for the stage kernels: persistent grids of resident blocks.
+// block_size (0 = defaults 256/128) sets the shade-type blocks; the trace
+// kernels use min(block_size, 128).
+template <bool BATCH>
+Launch make_launch(pyre_ctx* ctx, uint32_t block_size) {
+    Launch L;
+    if (block_size) {
+        const int b = (int)std::max(32u, std::min(256u, block_size / 32 * 32));
+        L.block_shade = b;
+        L.block_trace = std::min(b, 128);
+    }
+    L.grid_raygen = grid_for(ctx, k_raygen<BATCH>, L.block_shade);
+    L.grid_shade = grid_for(ctx, k_shade<BATCH>, L.block_shade);
+    L.grid_extend = grid_for(ctx, k_extend<BATCH>, L.block_trace);
+    L.grid_shadow = grid_for(ctx, k_shadow<BATCH>, L.block_trace);
+    L.grid_acc = BATCH ? grid_for(ctx, k_accumulate_batch, L.block_shade) : grid_for(ctx, k_accumulate, L.block_shade);
+    return L;
+}
 
 // Stage timing (off by default): an event before each stage kernel, tagged
 // with that kernel's stage; durations are differences of consecutive events.
@@ -699,19 +719,19 @@ void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Wave
     cudaStream_t st = ctx->stream;
     mark(ctx, STAGE_OTHER);
     k_wave_begin<<<1, 32, 0, st>>>(P.ctl, W.spp_begin, W.spp_end, W.k_per_wave, W.npix);
-    k_raygen<false><<<Lc.grid_raygen, 256, 0, st>>>(P, W);
+    k_raygen<false><<<Lc.grid_raygen, Lc.block_shade, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
-        k_extend<false><<<Lc.grid_extend, 128, 0, st>>>(S, P, W, d);
+        k_extend<false><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
         mark(ctx, STAGE_SHADE);
-        k_shade<false><<<Lc.grid_shade, 256, 0, st>>>(S, P, W, d);
+        k_shade<false><<<Lc.grid_shade, Lc.block_shade, 0, st>>>(S, P, W, d);
         if (W.ns > 0) {
             mark(ctx, STAGE_SHADOW);
-            k_shadow<false><<<Lc.grid_shadow, 128, 0, st>>>(S, P, W, d);
+            k_shadow<false><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
         }
     }
     mark(ctx, STAGE_OTHER);
-    k_accumulate<<<Lc.grid_acc, 256, 0, st>>>(P, W);
+    k_accumulate<<<Lc.grid_acc, Lc.block_shade, 0, st>>>(P, W);
     k_wave_end<<<1, 32, 0, st>>>(P.ctl, W.max_depth);
     mark(ctx, STAGE_END);
 }
@@ -722,19 +742,19 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
     cudaStream_t st = ctx->stream;
     mark(ctx, STAGE_OTHER);
     k_wave_begin_batch<<<1, 32, 0, st>>>(P.ctl, W.waves);
-    k_raygen<true><<<Lc.grid_raygen, 256, 0, st>>>(P, W);
+    k_raygen<true><<<Lc.grid_raygen, Lc.block_shade, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
-        k_extend<true><<<Lc.grid_extend, 128, 0, st>>>(S, P, W, d);
+        k_extend<true><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
         mark(ctx, STAGE_SHADE);
-        k_shade<true><<<Lc.grid_shade, 256, 0, st>>>(S, P, W, d);
+        k_shade<true><<<Lc.grid_shade, Lc.block_shade, 0, st>>>(S, P, W, d);
         if (W.ns > 0) {
             mark(ctx, STAGE_SHADOW);
-            k_shadow<true><<<Lc.grid_shadow, 128, 0, st>>>(S, P, W, d);
+            k_shadow<true><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
         }
     }
     mark(ctx, STAGE_OTHER);
-    k_accumulate_batch<<<Lc.grid_acc, 256, 0, st>>>(P, W);
+    k_accumulate_batch<<<Lc.grid_acc, Lc.block_shade, 0, st>>>(P, W);
     k_wave_end<<<1, 32, 0, st>>>(P.ctl, W.max_depth);
     mark(ctx, STAGE_END);
 }
@@ -792,12 +812,7 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
     carve_paths((char*)ctx->render_ws.ptr, P, std::max(W.ns, 1u), W.npix, &S);
     if (film->mem == PYRE_MEM_HOST && (rc = ensure_workspace(ctx, ctx->io_ws, film_bytes))) return rc;
 
-    Launch Lc;
-    Lc.grid_raygen = grid_for(ctx, k_raygen<false>, 256);
-    Lc.grid_shade = grid_for(ctx, k_shade<false>, 256);
-    Lc.grid_extend = grid_for(ctx, k_extend<false>, 128);
-    Lc.grid_shadow = grid_for(ctx, k_shadow<false>, 128);
-    Lc.grid_acc = grid_for(ctx, k_accumulate, 256);
+    const Launch Lc = make_launch<false>(ctx, rp.block_size);
 
     cudaStream_t st = ctx->stream;
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_r, 0, (size_t)W.npix * sizeof(float4), st));
@@ -814,7 +829,8 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
         std::snprintf(key, sizeof key, "%llu/%p/%u/%u/%u/%u/%u/%u/%u/%u/%d", (unsigned long long)scene->serial, ctx->render_ws.ptr,
                       W.npix, W.k_per_wave, W.max_depth, W.min_rr, W.ns, W.spp_begin, W.spp_end, W.cx0 + W.cy0 * 65536u,
                       W.env_cdf);
-        std::string k2 = std::string(key) + "/" + std::to_string(W.width) + "x" + std::to_string(W.height);
+        std::string k2 = std::string(key) + "/" + std::to_string(W.width) + "x" + std::to_string(W.height) + "/b" +
+                         std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace);
         // camera bytes are part of the key
         k2.append(reinterpret_cast<const char*>(&W.cam), sizeof(W.cam));
         if (!ctx->wave_graph || ctx->wave_graph_key != k2) {
@@ -984,12 +1000,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_n, 0, total_pix * sizeof(float4), st));
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
 
-    Launch Lc;
-    Lc.grid_raygen = grid_for(ctx, k_raygen<true>, 256);
-    Lc.grid_shade = grid_for(ctx, k_shade<true>, 256);
-    Lc.grid_extend = grid_for(ctx, k_extend<true>, 128);
-    Lc.grid_shadow = grid_for(ctx, k_shadow<true>, 128);
-    Lc.grid_acc = grid_for(ctx, k_accumulate_batch, 256);
+    const Launch Lc = make_launch<true>(ctx, params ? params->block_size : 0u);
 
     PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
     ctx->stage_used = 0;
@@ -998,7 +1009,8 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
         // The whole batch (every wave) as one graph, launched once.
         std::string key = "batch/" + std::to_string(scene->serial) + "/" +
                           std::to_string((uintptr_t)ctx->render_ws.ptr) + "/" + std::to_string(n_waves) + "/" +
-                          std::to_string(max_depth) + "/" + std::to_string(max_paths) + "/";
+                          std::to_string(max_depth) + "/" + std::to_string(max_paths) + "/b" +
+                          std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace) + "/";
         key.append(reinterpret_cast<const char*>(dj.data()), job_bytes);
         if (!ctx->wave_graph || ctx->wave_graph_key != key) {
             if (ctx->wave_graph) { cudaGraphExecDestroy(ctx->wave_graph); ctx->wave_graph = nullptr; }

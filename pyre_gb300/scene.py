@@ -364,13 +364,13 @@ class CudaIntegrator:
 
     @staticmethod
     def params(width, height, spp_begin, spp_end, integrator: PathIntegrator, crop=None, env_sampling=0,
-               wave_paths=0, use_graph=0) -> N.RenderParams:
+               wave_paths=0, use_graph=0, block_size=0) -> N.RenderParams:
         p = N.RenderParams()
         p.width, p.height, p.spp_begin, p.spp_end = width, height, spp_begin, spp_end
         p.max_depth, p.min_rr_depth = integrator.max_depth, integrator.min_rr_depth
         if crop is not None:
             p.crop[:] = list(crop)
-        p.env_sampling, p.wave_paths, p.use_graph = env_sampling, wave_paths, use_graph
+        p.env_sampling, p.wave_paths, p.use_graph, p.block_size = env_sampling, wave_paths, use_graph, block_size
         return p
 
     def render(self, dscene: DeviceScene, camera: CameraSpec, integrator: PathIntegrator, width: int, height: int,
@@ -393,7 +393,8 @@ class CudaIntegrator:
         self.check(self.lib.pyre_scene_upload_batch(self.handle, arr, len(flats), C.byref(h)))
         return DeviceScene(self, h, scenes)
 
-    def render_batch(self, dscene: DeviceScene, jobs: list, wave_paths: int = 0, use_graph: int = 0) -> list:
+    def render_batch(self, dscene: DeviceScene, jobs: list, wave_paths: int = 0, use_graph: int = 0,
+                     block_size: int = 0) -> list:
         """jobs: dicts with part, camera, width, height, spp, spp_begin (0), integrator -> list of Films."""
         films, cjobs = [], []
         for jb in jobs:
@@ -413,7 +414,7 @@ class CudaIntegrator:
             cjobs.append(b)
         arr = (N.BatchJob * len(cjobs))(*cjobs)
         p = N.RenderParams()
-        p.wave_paths, p.use_graph = wave_paths, use_graph
+        p.wave_paths, p.use_graph, p.block_size = wave_paths, use_graph, block_size
         self.check(self.lib.pyre_render_batch(self.handle, dscene.handle, arr, len(cjobs), C.byref(p)))
         return films
 
