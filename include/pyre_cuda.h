@@ -255,6 +255,37 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
                 const pyre_render_params* params, pyre_film* film);
 int pyre_get_render_stats(const pyre_ctx* ctx, pyre_render_stats* out);
 
+/* ----------------------------------------------------------- Adjoint --- */
+
+/* Gradients of a scalar loss. materials: n_materials * 6 doubles,
+ * d loss / d (base_color r, g, b, metallic, roughness, specular) per
+ * material (a Lambertian's albedo is its base color; its other three entries
+ * stay zero). env: width * height * 3 floats, d loss / d texel RGB (row 0 =
+ * zenith), or NULL. Both are overwritten. */
+typedef struct pyre_gradients {
+    double* materials;
+    float* env;
+    int mem; /* PYRE_MEM_HOST or PYRE_MEM_DEVICE */
+} pyre_gradients;
+
+/* Path-replay adjoint of pyre_render (no reference counterpart: the
+ * reference has no differentiation). Given d loss / d film radiance for the
+ * render with the same camera and params (crop-sized, RGB per pixel), it
+ * re-traces every path of the sample range from its pixel seed and writes
+ * the gradients. Convention: detached sampling; only BSDF values and emitted
+ * radiance carry derivatives (pdfs, MIS weights, lobe choice, Russian
+ * roulette and the environment's sampling tables are constants), which is
+ * unbiased for the derivative of the expected image. Limits: max_depth <= 16,
+ * at most 3 quad lights, single (non-batch) scenes. */
+int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                  const pyre_render_params* params, const float* d_loss_d_image, int image_mem,
+                  pyre_gradients* grads);
+
+/* Replaces the materials of an uploaded scene in place (same count). */
+int pyre_scene_set_materials(pyre_ctx* ctx, pyre_scene* scene, const pyre_material_desc* materials, uint32_t n);
+/* Replaces the environment texels (same size) and rebuilds its sampling tables. */
+int pyre_scene_set_env(pyre_ctx* ctx, pyre_scene* scene, const float* rgb, float intensity);
+
 /* ------------------------------------------------------------- Batch --- */
 
 /* Uploads n_parts scenes as one device scene (shared arrays, one top-level

@@ -58,6 +58,8 @@ _SIG = {
     "orc_render_one": (None, [C.c_void_p, P_f, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                               C.c_uint32, C.c_uint32, P_f]),
     "orc_num_threads": (C.c_int, []),
+    "orc_render_grad": (None, [C.c_void_p, P_f, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                               C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, P_f, P_d, C.c_int]),
 }
 
 _lib = None
@@ -272,6 +274,20 @@ class OracleScene:
                              x0, y0, x1, y1, self.nthreads, _f(rgb), _f(alb), _f(nor), _f(dep),
                              acc.ctypes.data_as(P_d) if acc is not None else None)
         return {"radiance": rgb, "albedo": alb, "normal": nor, "depth": dep, "bounces": int(b), "accum64": acc}
+
+    def render_grad(self, camera, width, height, spp, dl_di, n_materials, env_shape=None, spp_begin=0, crop=None,
+                    max_depth=8, min_rr_depth=3):
+        """Forward-mode (dual-number) gradient of a loss with d loss / d film = dl_di (crop h, w, 3).
+        Returns (material grads (n_materials, 6), env grads (h, w, 3) or None)."""
+        x0, y0, x1, y1 = crop if crop is not None else (0, 0, width, height)
+        d = _c(dl_di).reshape(-1)
+        n_env = 0 if env_shape is None else env_shape[0] * env_shape[1] * 3
+        out = np.zeros(n_materials * 6 + n_env, np.float64)
+        lib().orc_render_grad(self.h, _f(camera.as_array()), width, height, spp_begin, spp_begin + spp, max_depth,
+                              min_rr_depth, x0, y0, x1, y1, _f(d), out.ctypes.data_as(P_d), self.nthreads)
+        mat = out[: n_materials * 6].reshape(n_materials, 6)
+        env = out[n_materials * 6:].reshape(env_shape[0], env_shape[1], 3) if env_shape is not None else None
+        return mat, env
 
     def render_one(self, camera, width, height, x, y, s, max_depth=8, min_rr_depth=3):
         out = np.zeros(10, F32)

@@ -836,7 +836,7 @@ struct Env {  // HdriEnvironmentLight, light.rs:205-350
 // Scene — crates/pyre/src/scene.rs:19-152
 // ---------------------------------------------------------------------------
 struct SceneHit {
-    Hit hit; int is_light; uint32_t id; uint32_t material_id;
+    Hit hit; int is_light = 0; uint32_t id = 0; uint32_t material_id = 0;
 };
 
 struct Scene {
@@ -1020,6 +1020,237 @@ static PixelSample render_sample(const Scene& scene, const Camera& cam, uint32_t
     float time = sampler.next_f32();
     Ray ray = cam.generate_ray(ndc, lens, time);
     return integrate(ray, scene, sampler, max_depth, min_rr, bounces);
+}
+
+// ---------------------------------------------------------------------------
+// Forward-mode gradient of the integrator (no reference counterpart).
+//
+// Same path as integrate() (same sampler draws and decisions), with the
+// detached-sampling convention: the BSDF values f (throughput and NEE) and
+// the emitted environment radiance carry derivatives; pdfs, MIS weights,
+// lobe choice, Russian roulette and the environment's sampling tables are
+// constants. Tangents are all material parameters (6 per material: base
+// r,g,b, metallic, roughness, specular) followed by all environment texels
+// (3 per texel). The throughput carries a dense tangent vector per channel.
+// ---------------------------------------------------------------------------
+struct Dual6 {
+    float v; float d[6];
+    Dual6() : v(0) { for (float& x : d) x = 0; }
+    Dual6(float a) : v(a) { for (float& x : d) x = 0; }
+    static Dual6 var(float a, int k) { Dual6 r(a); r.d[k] = 1.0f; return r; }
+};
+static inline Dual6 operator+(Dual6 a, Dual6 b) { Dual6 r(a.v + b.v); for (int k = 0; k < 6; ++k) r.d[k] = a.d[k] + b.d[k]; return r; }
+static inline Dual6 operator-(Dual6 a, Dual6 b) { Dual6 r(a.v - b.v); for (int k = 0; k < 6; ++k) r.d[k] = a.d[k] - b.d[k]; return r; }
+static inline Dual6 operator*(Dual6 a, Dual6 b) { Dual6 r(a.v * b.v); for (int k = 0; k < 6; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k]; return r; }
+static inline Dual6 operator/(Dual6 a, Dual6 b) {
+    Dual6 r(a.v / b.v);
+    for (int k = 0; k < 6; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v);
+    return r;
+}
+static inline Dual6 dsqrt(Dual6 a) {
+    Dual6 r(std::sqrt(a.v));
+    for (int k = 0; k < 6; ++k) r.d[k] = r.v > 0 ? a.d[k] / (2.0f * r.v) : 0.0f;
+    return r;
+}
+
+// f(wo, wi) and J[c][k] = d f_c / d param_k (material.rs:52-58, 125-155).
+static void eval_jacobian(const Material& m, V3 wo, V3 wi, float J[3][6]) {
+    for (int c = 0; c < 3; ++c) for (int k = 0; k < 6; ++k) J[c][k] = 0.0f;
+    if (m.kind == MAT_LAMBERTIAN) {
+        if (wo.z <= 0.0f || wi.z <= 0.0f) return;
+        J[0][0] = J[1][1] = J[2][2] = 1.0f / PI;
+        return;
+    }
+    Dual6 base[3] = {Dual6::var(m.albedo.x, 0), Dual6::var(m.albedo.y, 1), Dual6::var(m.albedo.z, 2)};
+    Dual6 metal = Dual6::var(m.metallic, 3), rough = Dual6::var(m.roughness, 4), spec = Dual6::var(m.specular, 5);
+    Dual6 f[3];
+    if (!(wo.z <= 0.0f || wi.z <= 0.0f || m.metallic >= 1.0f)) {
+        V3 h = normalize_or_zero(wo + wi);
+        if (!(length_squared(h) < 1e-10f)) {
+            float cos_d = clampf(dot(wi, h), 0.0f, 1.0f);
+            Dual6 fd90 = Dual6(0.5f) + Dual6(2.0f) * rough * Dual6(cos_d) * Dual6(cos_d);
+            Dual6 fd_v = Dual6(1.0f) + (fd90 - Dual6(1.0f)) * Dual6(powi5(fmax_(1.0f - wo.z, 0.0f)));
+            Dual6 fd_l = Dual6(1.0f) + (fd90 - Dual6(1.0f)) * Dual6(powi5(fmax_(1.0f - wi.z, 0.0f)));
+            for (int c = 0; c < 3; ++c) f[c] = base[c] * (Dual6(1.0f) - metal) / Dual6(PI) * fd_v * fd_l;
+        }
+    }
+    if (!(wo.z <= 0.0f || wi.z <= 0.0f)) {
+        V3 h = normalize_or_zero(wo + wi);
+        if (!(length_squared(h) < 1e-10f || h.z <= 0.0f)) {
+            Dual6 r2 = rough * rough;
+            Dual6 alpha = r2.v >= 1e-3f ? r2 : Dual6(1e-3f);
+            Dual6 a2 = alpha * alpha;
+            Dual6 denom = Dual6(h.z * h.z) * (a2 - Dual6(1.0f)) + Dual6(1.0f);
+            Dual6 D = a2 / (Dual6(PI) * denom * denom);
+            auto lambda = [&](V3 v) {
+                float cos2 = v.z * v.z;
+                if (cos2 >= 1.0f) return Dual6(0.0f);
+                float tan2 = (1.0f - cos2) / fmax_(cos2, 1e-8f);
+                return Dual6(0.5f) * (Dual6(-1.0f) + dsqrt(Dual6(1.0f) + a2 * Dual6(tan2)));
+            };
+            Dual6 G = Dual6(1.0f) / (Dual6(1.0f) + lambda(wo) + lambda(wi));
+            float c5 = powi5(1.0f - clampf(fmax_(dot(wi, h), 0.0f), 0.0f, 1.0f));
+            Dual6 diel = Dual6(0.08f) * spec;
+            for (int c = 0; c < 3; ++c) {
+                Dual6 f0 = diel * (Dual6(1.0f) - metal) + base[c] * metal;
+                Dual6 F = f0 + (Dual6(1.0f) - f0) * Dual6(c5);
+                f[c] = f[c] + D * F * G / Dual6(4.0f * wo.z * wi.z);
+            }
+        }
+    }
+    for (int c = 0; c < 3; ++c) for (int k = 0; k < 6; ++k) J[c][k] = f[c].d[k];
+}
+
+// Bilinear texel weights of Env::sample_texture (light.rs:290-314).
+static void texel_weights(const Env& e, V2 uv, uint32_t idx[4], float wt[4]) {
+    int32_t w = (int32_t)e.width, h = (int32_t)e.height;
+    float u = Env::fract(Env::fract(uv.x) + 1.0f);
+    float v = clampf(uv.y, 0.0f, 1.0f);
+    float fx = u * (float)w - 0.5f;
+    float fy = clampf(v * (float)h - 0.5f, 0.0f, (float)h - 1.0f);
+    int32_t x0i = Env::as_i32(std::floor(fx)), y0i = Env::as_i32(std::floor(fy));
+    float dx = fx - (float)x0i, dy = fy - (float)y0i;
+    int32_t x0 = Env::rem_euclid(x0i, w), x1 = Env::rem_euclid(x0 + 1, w);
+    int32_t y0 = std::min(std::max(y0i, 0), h - 1), y1 = std::min(y0 + 1, h - 1);
+    idx[0] = (uint32_t)(y0 * w + x0); wt[0] = (1.0f - dx) * (1.0f - dy);
+    idx[1] = (uint32_t)(y0 * w + x1); wt[1] = dx * (1.0f - dy);
+    idx[2] = (uint32_t)(y1 * w + x0); wt[2] = (1.0f - dx) * dy;
+    idx[3] = (uint32_t)(y1 * w + x1); wt[3] = dx * dy;
+}
+
+struct GradPath {
+    size_t n;                    // tangent count
+    std::vector<double> beta_d;  // 3 * n: d beta_c / d theta
+    std::vector<double>* grad;   // accumulates delta . dL/dtheta
+};
+
+// d(loss) of a term  beta (x) f (x) k  where f carries material m's
+// Jacobian J (or none), plus an environment texture factor.
+static void add_term(GradPath& G, V3 beta, V3 f, V3 k, V3 delta, int mat, const float (*J)[6],
+                     size_t env_base, const Env* env, V2 uv, V3 kenv) {
+    const float dv[3] = {delta.x, delta.y, delta.z}, bv[3] = {beta.x, beta.y, beta.z}, fv[3] = {f.x, f.y, f.z},
+                kv[3] = {k.x, k.y, k.z};
+    std::vector<double>& g = *G.grad;
+    for (int c = 0; c < 3; ++c) {
+        const double s = (double)dv[c] * fv[c] * kv[c];
+        if (s != 0.0) {
+            const double* bd = &G.beta_d[(size_t)c * G.n];
+            for (size_t t = 0; t < G.n; ++t) g[t] += s * bd[t];
+        }
+        if (J && mat >= 0) {
+            const double w = (double)dv[c] * bv[c] * kv[c];
+            for (int p = 0; p < 6; ++p) g[(size_t)mat * 6 + p] += w * J[c][p];
+        }
+    }
+    if (env) {  // term beta * kenv * texture(uv) * intensity
+        uint32_t idx[4]; float wt[4];
+        texel_weights(*env, uv, idx, wt);
+        const float ke[3] = {kenv.x, kenv.y, kenv.z};
+        for (int q = 0; q < 4; ++q)
+            for (int c = 0; c < 3; ++c)
+                g[env_base + 3 * (size_t)idx[q] + c] += (double)dv[c] * bv[c] * ke[c] * wt[q] * env->intensity;
+    }
+}
+
+static void integrate_grad(Ray ray, const Scene& scene, Sampler& sampler, uint32_t max_depth, uint32_t min_rr,
+                           V3 delta, GradPath& G) {
+    const size_t env_base = scene.materials.size() * 6;
+    V3 beta(1, 1, 1);
+    std::fill(G.beta_d.begin(), G.beta_d.end(), 0.0);
+    float last_pdf_bsdf = 0.0f;
+    bool last_was_specular = true;
+    for (uint32_t depth = 0; depth < max_depth; ++depth) {
+        SceneHit hit;
+        if (!scene.intersect(ray, &hit, 0)) {
+            if (scene.has_env) {
+                V3 le = scene.env.le(ray.direction);
+                if (le != V3()) {
+                    float w = last_was_specular ? 1.0f
+                                                : power_heuristic(last_pdf_bsdf, scene.env.pdf(ray.direction));
+                    // term beta * le * w, le = texture * intensity
+                    add_term(G, beta, le, V3(w, w, w), delta, -1, nullptr, env_base, &scene.env,
+                             Env::dir_to_uv(ray.direction), V3(w, w, w));
+                }
+            }
+            break;
+        }
+        if (hit.is_light) {
+            const QuadLight& light = scene.lights[hit.id];
+            V3 le = light.le(hit.hit.normal, -ray.direction);
+            float w = last_was_specular ? 1.0f : power_heuristic(last_pdf_bsdf, light.pdf(ray.origin, ray.direction));
+            add_term(G, beta, le, V3(w, w, w), delta, -1, nullptr, 0, nullptr, V2(), V3());
+            break;
+        }
+        const Material& material = scene.materials[hit.material_id];
+        const int mat = (int)hit.material_id;
+        V3 p = hit.hit.position, ns = hit.hit.normal;
+        Frame frame = Frame::from_normal(ns);
+        V3 wo_local = frame.to_local(-ray.direction);
+        if (wo_local.z <= 0.0f) break;
+        for (const QuadLight& light : scene.lights) {
+            V2 u = sampler.next_vec2();
+            V3 lpos, lwi, lli; float lpdf;
+            if (!light.sample(p, u, &lpos, &lwi, &lpdf, &lli)) continue;
+            if (lpdf <= 0.0f || lli == V3()) continue;
+            V3 wi_local = frame.to_local(lwi);
+            if (wi_local.z <= 0.0f) continue;
+            V3 f = material.eval(wo_local, wi_local);
+            if (f == V3()) continue;
+            if (scene.occluded(p + RAY_EPS * ns, lpos - RAY_EPS * lwi, ray.time)) continue;
+            float w = power_heuristic(lpdf, material.pdf(wo_local, wi_local));
+            float J[3][6];
+            eval_jacobian(material, wo_local, wi_local, J);
+            add_term(G, beta, f, lli * wi_local.z * w / lpdf, delta, mat, J, 0, nullptr, V2(), V3());
+        }
+        if (scene.has_env) {
+            V2 u = sampler.next_vec2();
+            V3 ewi, eli; float epdf;
+            scene.env.sample(u, &ewi, &eli, &epdf);
+            if (epdf > 0.0f && eli != V3()) {
+                V3 wi_local = frame.to_local(ewi);
+                if (wi_local.z > 0.0f) {
+                    V3 f = material.eval(wo_local, wi_local);
+                    if (f != V3() && !scene.occluded_dir(p + RAY_EPS * ns, ewi, ray.time)) {
+                        float w = power_heuristic(epdf, material.pdf(wo_local, wi_local));
+                        float k = wi_local.z * w / epdf;
+                        float J[3][6];
+                        eval_jacobian(material, wo_local, wi_local, J);
+                        add_term(G, beta, f, eli * k, delta, mat, J, env_base, &scene.env,
+                                 Env::dir_to_uv(ewi), f * k);
+                    }
+                }
+            }
+        }
+        V3 bwi, bf; float bpdf;
+        if (!material.sample(wo_local, sampler.next_vec2(), &bwi, &bf, &bpdf)) break;
+        if (bpdf <= 0.0f) break;
+        float cos_wi = std::fabs(bwi.z);
+        if (cos_wi == 0.0f) break;
+        float a = cos_wi / bpdf;
+        V3 nbeta = beta * (bf * cos_wi / bpdf);
+        if (depth >= min_rr) {
+            float q = clampf(1.0f - max_element(nbeta), 0.05f, 0.95f);
+            if (sampler.next_f32() < q) break;
+            nbeta = nbeta / (1.0f - q);
+            a = a / (1.0f - q);
+        }
+        // d beta' = d beta * f * a + beta * a * df
+        float J[3][6];
+        eval_jacobian(material, wo_local, bwi, J);
+        const float fv[3] = {bf.x, bf.y, bf.z}, bv[3] = {beta.x, beta.y, beta.z};
+        for (int c = 0; c < 3; ++c) {
+            double* bd = &G.beta_d[(size_t)c * G.n];
+            const double s = (double)fv[c] * a;
+            for (size_t t = 0; t < G.n; ++t) bd[t] *= s;
+            for (int q = 0; q < 6; ++q) bd[(size_t)mat * 6 + q] += (double)bv[c] * a * J[c][q];
+        }
+        beta = nbeta;
+        last_pdf_bsdf = bpdf;
+        last_was_specular = false;
+        Ray nr; nr.origin = p + RAY_EPS * ns; nr.direction = frame.to_world(bwi);
+        nr.t_min = 1e-4f; nr.t_max = INF; nr.time = ray.time;
+        ray = nr;
+    }
 }
 
 }  // namespace orc
@@ -1329,6 +1560,55 @@ uint64_t orc_render(void* s, const float* cam, uint32_t width, uint32_t height, 
         }
     }
     return total;
+}
+
+// Forward-mode gradient of the render's loss: dl_di (crop*3) is d loss / d
+// film radiance; grad_out (n_mat*6 + env texels*3) receives the gradient.
+void orc_render_grad(void* s, const float* cam, uint32_t width, uint32_t height, uint32_t spp_begin,
+                     uint32_t spp_end, uint32_t max_depth, uint32_t min_rr_depth, uint32_t x0, uint32_t y0,
+                     uint32_t x1, uint32_t y1, const float* dl_di, double* grad_out, int nthreads) {
+    Scene* sc = (Scene*)s;
+    Camera c = cam_from(cam);
+    const uint32_t cw = x1 - x0, ch = y1 - y0;
+    const size_t n = sc->materials.size() * 6 + (sc->has_env ? (size_t)sc->env.width * sc->env.height * 3 : 0);
+    const float inv_spp = 1.0f / (float)(spp_end - spp_begin);
+    std::vector<double> total(n, 0.0);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+#endif
+    {
+        std::vector<double> local(n, 0.0);
+        GradPath G;
+        G.n = n;
+        G.beta_d.assign(3 * n, 0.0);
+        G.grad = &local;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 4)
+#endif
+        for (int64_t pix = 0; pix < (int64_t)cw * ch; ++pix) {
+            const uint32_t xx = (uint32_t)(pix % cw), yy = (uint32_t)(pix / cw);
+            const uint32_t x = x0 + xx, y = y0 + yy;
+            V3 delta(dl_di[3 * pix] * inv_spp, dl_di[3 * pix + 1] * inv_spp, dl_di[3 * pix + 2] * inv_spp);
+            if (delta == V3()) continue;
+            for (uint32_t sidx = spp_begin; sidx < spp_end; ++sidx) {
+                Sampler sampler(pixel_seed(x, y, sidx));
+                float jx = sampler.next_f32(), jy = sampler.next_f32();
+                V2 ndc;
+                ndc.x = 2.0f * ((float)x + jx) / (float)width - 1.0f;
+                ndc.y = 1.0f - 2.0f * ((float)y + jy) / (float)height;
+                V2 lens = sampler.next_vec2();
+                float time = sampler.next_f32();
+                Ray ray = c.generate_ray(ndc, lens, time);
+                integrate_grad(ray, *sc, sampler, max_depth, min_rr_depth, delta, G);
+            }
+        }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+        for (size_t k = 0; k < n; ++k) total[k] += local[k];
+    }
+    for (size_t k = 0; k < n; ++k) grad_out[k] = total[k];
 }
 
 // Single sample for path-level debugging.

@@ -127,6 +127,48 @@ void build_alias(const float* cdf, uint32_t n, float2* table) {
     for (uint32_t i : large) table[i].x = 1.0f;
 }
 
+// Environment texels and sampling tables of HdriEnvironmentLight::new
+// (light.rs:214-242): weights lum * sin(theta_row), Distribution2D CDFs,
+// per-bin pdfs and alias tables.
+struct EnvTables {
+    std::vector<float4> px;
+    std::vector<float> marg_cdf, cond_cdf, marg_pdf, cond_pdf;
+    std::vector<float2> marg_alias, cond_alias;
+};
+
+void build_env_tables(uint32_t w, uint32_t h, const float* rgb, EnvTables& t) {
+    t.px.resize((size_t)w * h);
+    std::vector<float> weights((size_t)w * h);
+    for (uint32_t y = 0; y < h; ++y) {
+        float theta = ((float)y + 0.5f) / (float)h * 3.14159265358979323846f;
+        float sin_theta = std::fmax(std::sin(theta), 0.0f);
+        for (uint32_t x = 0; x < w; ++x) {
+            const float* p = rgb + 3 * ((size_t)y * w + x);
+            t.px[(size_t)y * w + x] = make_float4(p[0], p[1], p[2], 0.0f);
+            float lum = 0.21267f * p[0] + 0.71516f * p[1] + 0.07217f * p[2];
+            weights[(size_t)y * w + x] = std::fmax(lum, 0.0f) * sin_theta;
+        }
+    }
+    t.cond_cdf.resize((size_t)h * (w + 1));
+    t.cond_pdf.resize((size_t)w * h);
+    t.cond_alias.resize((size_t)w * h);
+    std::vector<float> row_integral(h);
+    for (uint32_t y = 0; y < h; ++y) {
+        float* cdf = t.cond_cdf.data() + (size_t)y * (w + 1);
+        row_integral[y] = build_cdf(weights.data() + (size_t)y * w, w, cdf);
+        for (uint32_t x = 0; x < w; ++x) t.cond_pdf[(size_t)y * w + x] = (cdf[x + 1] - cdf[x]) * (float)w;
+        build_alias(cdf, w, t.cond_alias.data() + (size_t)y * w);
+    }
+    t.marg_cdf.resize(h + 1);
+    t.marg_pdf.resize(h);
+    t.marg_alias.resize(h);
+    build_cdf(row_integral.data(), h, t.marg_cdf.data());
+    for (uint32_t y = 0; y < h; ++y) t.marg_pdf[y] = (t.marg_cdf[y + 1] - t.marg_cdf[y]) * (float)h;
+    build_alias(t.marg_cdf.data(), h, t.marg_alias.data());
+}
+
+std::atomic<uint64_t> g_scene_serial{1};
+
 }  // namespace
 }  // namespace pyre
 
@@ -258,8 +300,7 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     }
 
     pyre_scene* sc = new pyre_scene();
-    static std::atomic<uint64_t> serial{1};
-    sc->serial = serial++;
+    sc->serial = g_scene_serial++;
     auto fail = [&](int rc) { pyre_scene_destroy(ctx, sc); return rc; };
 
     // ---- collapse BVHs, lay out triangle slots, index and normal buffers
@@ -401,42 +442,12 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     }
 
     // ---- environment: texels, CDFs, per-bin pdfs, alias tables (light.rs:214-242)
-    std::vector<float4> env_px;
-    std::vector<float> marg_cdf, cond_cdf, marg_pdf, cond_pdf;
-    std::vector<float2> marg_alias, cond_alias;
+    EnvTables et;
     DevEnv env{};
     if (desc->env) {
-        const uint32_t w = desc->env->width, h = desc->env->height;
-        env_px.resize((size_t)w * h);
-        std::vector<float> weights((size_t)w * h);
-        for (uint32_t y = 0; y < h; ++y) {
-            float theta = ((float)y + 0.5f) / (float)h * 3.14159265358979323846f;
-            float sin_theta = std::fmax(std::sin(theta), 0.0f);
-            for (uint32_t x = 0; x < w; ++x) {
-                const float* p = desc->env->rgb + 3 * ((size_t)y * w + x);
-                env_px[(size_t)y * w + x] = make_float4(p[0], p[1], p[2], 0.0f);
-                float lum = 0.21267f * p[0] + 0.71516f * p[1] + 0.07217f * p[2];
-                weights[(size_t)y * w + x] = std::fmax(lum, 0.0f) * sin_theta;
-            }
-        }
-        cond_cdf.resize((size_t)h * (w + 1));
-        cond_pdf.resize((size_t)w * h);
-        cond_alias.resize((size_t)w * h);
-        std::vector<float> row_integral(h);
-        for (uint32_t y = 0; y < h; ++y) {
-            float* cdf = cond_cdf.data() + (size_t)y * (w + 1);
-            row_integral[y] = build_cdf(weights.data() + (size_t)y * w, w, cdf);
-            for (uint32_t x = 0; x < w; ++x) cond_pdf[(size_t)y * w + x] = (cdf[x + 1] - cdf[x]) * (float)w;
-            build_alias(cdf, w, cond_alias.data() + (size_t)y * w);
-        }
-        marg_cdf.resize(h + 1);
-        marg_pdf.resize(h);
-        marg_alias.resize(h);
-        build_cdf(row_integral.data(), h, marg_cdf.data());
-        for (uint32_t y = 0; y < h; ++y) marg_pdf[y] = (marg_cdf[y + 1] - marg_cdf[y]) * (float)h;
-        build_alias(marg_cdf.data(), h, marg_alias.data());
-        env.width = w;
-        env.height = h;
+        build_env_tables(desc->env->width, desc->env->height, desc->env->rgb, et);
+        env.width = desc->env->width;
+        env.height = desc->env->height;
         env.intensity = desc->env->intensity;
     }
 
@@ -485,10 +496,10 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
         float4* px = nullptr;
         float *mc = nullptr, *cc = nullptr, *mp = nullptr, *cp = nullptr;
         float2 *ma = nullptr, *ca = nullptr;
-        if ((rc = upload(ctx, sc, env_px, &px)) != PYRE_OK || (rc = upload(ctx, sc, marg_cdf, &mc)) != PYRE_OK ||
-            (rc = upload(ctx, sc, cond_cdf, &cc)) != PYRE_OK || (rc = upload(ctx, sc, marg_pdf, &mp)) != PYRE_OK ||
-            (rc = upload(ctx, sc, cond_pdf, &cp)) != PYRE_OK || (rc = upload(ctx, sc, marg_alias, &ma)) != PYRE_OK ||
-            (rc = upload(ctx, sc, cond_alias, &ca)) != PYRE_OK)
+        if ((rc = upload(ctx, sc, et.px, &px)) != PYRE_OK || (rc = upload(ctx, sc, et.marg_cdf, &mc)) != PYRE_OK ||
+            (rc = upload(ctx, sc, et.cond_cdf, &cc)) != PYRE_OK || (rc = upload(ctx, sc, et.marg_pdf, &mp)) != PYRE_OK ||
+            (rc = upload(ctx, sc, et.cond_pdf, &cp)) != PYRE_OK || (rc = upload(ctx, sc, et.marg_alias, &ma)) != PYRE_OK ||
+            (rc = upload(ctx, sc, et.cond_alias, &ca)) != PYRE_OK)
             return fail(rc);
         env.pixels = px; env.marg_cdf = mc; env.cond_cdf = cc; env.marg_pdf = mp; env.cond_pdf = cp;
         env.marg_alias = ma; env.cond_alias = ca;
@@ -548,6 +559,49 @@ int pyre_scene_upload_batch(pyre_ctx* ctx, const pyre_scene_desc* descs, uint32_
     merged.materials = mats.data(); merged.n_materials = (uint32_t)mats.size();
     merged.lights = lights.data(); merged.n_lights = (uint32_t)lights.size();
     return upload_parts(ctx, &merged, inst_part, light_part, n_parts, out);
+}
+
+int pyre_scene_set_materials(pyre_ctx* ctx, pyre_scene* scene, const pyre_material_desc* materials, uint32_t n) {
+    if (!ctx || !scene || (!materials && n)) return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_set_materials: NULL");
+    if (n != scene->dev.n_materials) return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_set_materials: count differs");
+    std::vector<DevMaterial> mats(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (materials[i].kind > PYRE_MAT_DISNEY) return set_error(ctx, PYRE_ERR_INVALID, "unknown material kind");
+        DevMaterial& d = mats[i];
+        for (int c = 0; c < 3; ++c) d.base[c] = materials[i].base_color[c];
+        d.kind = materials[i].kind; d.metallic = materials[i].metallic; d.roughness = materials[i].roughness;
+        d.specular = materials[i].specular; d.pad = 0;
+    }
+    cudaSetDevice(ctx->device);
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (n) PYRE_CUDA_TRY(ctx, cudaMemcpy((void*)scene->dev.materials, mats.data(), n * sizeof(DevMaterial),
+                                         cudaMemcpyHostToDevice));
+    return PYRE_OK;
+}
+
+int pyre_scene_set_env(pyre_ctx* ctx, pyre_scene* scene, const float* rgb, float intensity) {
+    if (!ctx || !scene || !rgb) return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_set_env: NULL argument");
+    if (!scene->dev.has_env) return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_set_env: the scene has no environment");
+    DevEnv& E = scene->dev.env;
+    EnvTables t;
+    build_env_tables(E.width, E.height, rgb, t);
+    cudaSetDevice(ctx->device);
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    auto put = [&](const void* dst, const void* src, size_t bytes) {
+        return cudaMemcpy(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice);
+    };
+    cudaError_t e;
+    if ((e = put(E.pixels, t.px.data(), t.px.size() * sizeof(float4))) != cudaSuccess ||
+        (e = put(E.marg_cdf, t.marg_cdf.data(), t.marg_cdf.size() * 4)) != cudaSuccess ||
+        (e = put(E.cond_cdf, t.cond_cdf.data(), t.cond_cdf.size() * 4)) != cudaSuccess ||
+        (e = put(E.marg_pdf, t.marg_pdf.data(), t.marg_pdf.size() * 4)) != cudaSuccess ||
+        (e = put(E.cond_pdf, t.cond_pdf.data(), t.cond_pdf.size() * 4)) != cudaSuccess ||
+        (e = put(E.marg_alias, t.marg_alias.data(), t.marg_alias.size() * sizeof(float2))) != cudaSuccess ||
+        (e = put(E.cond_alias, t.cond_alias.data(), t.cond_alias.size() * sizeof(float2))) != cudaSuccess)
+        return cuda_check(ctx, e, "pyre_scene_set_env");
+    E.intensity = intensity;
+    scene->serial = g_scene_serial++;  // cached graphs captured the old intensity
+    return PYRE_OK;
 }
 
 int pyre_scene_get_info(const pyre_scene* scene, pyre_scene_info* out) {

@@ -5,6 +5,7 @@
 // Transcendentals use CUDA's full-precision sinf/cosf/acosf/atan2f, which can
 // differ from glibc by an ulp; images are therefore compared statistically.
 #pragma once
+#include "../../include/pyre_cuda.h"
 #include "device_scene.cuh"
 
 namespace pyre {
@@ -361,6 +362,26 @@ __device__ __forceinline__ void camera_ray(const DevCamera& C, f2 ndc, f2 lens, 
     f3 lens_origin = C.origin + lens_offset;
     *o = lens_origin;
     *d = normalize3(normalize3(focal_point - lens_origin));
+}
+
+// Host side.
+inline DevCamera make_camera(const pyre_camera_desc& c) {
+    // PinholeCamera / ThinLensCamera::look_at (camera.rs:49-72, 105-122) on the host.
+    DevCamera d;
+    f3 origin = mk3(c.origin[0], c.origin[1], c.origin[2]);
+    f3 target = mk3(c.target[0], c.target[1], c.target[2]);
+    f3 up = mk3(c.up[0], c.up[1], c.up[2]);
+    d.origin = origin;
+    d.forward = normalize3(target - origin);
+    d.right = normalize3(cross3(d.forward, up));
+    d.up = cross3(d.right, d.forward);
+    const float to_rad = 3.14159265358979323846f / 180.0f;
+    d.half_height = std::tan(c.vfov_deg * to_rad / 2.0f);
+    d.half_width = c.aspect * d.half_height;
+    d.aperture_radius = c.aperture_radius;
+    d.focus_distance = c.focus_distance;
+    d.thin_lens = c.kind == PYRE_CAMERA_THIN_LENS ? 1 : 0;
+    return d;
 }
 
 }  // namespace pyre

@@ -109,6 +109,10 @@ class BatchJob(C.Structure):
                 ("min_rr_depth", C.c_uint32), ("film", Film)]
 
 
+class Gradients(C.Structure):
+    _fields_ = [("materials", C.POINTER(C.c_double)), ("env", P_f), ("mem", C.c_int)]
+
+
 class SceneInfo(C.Structure):
     _fields_ = [("n_triangles", C.c_uint64), ("n_nodes", C.c_uint64), ("n_instances", C.c_uint64),
                 ("triangle_bytes", C.c_uint64), ("node_bytes", C.c_uint64), ("device_bytes", C.c_uint64)]
@@ -138,6 +142,10 @@ SIGNATURES = {
     "pyre_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams),
                                       C.POINTER(Film)]),
     "pyre_set_stage_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "pyre_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams), P_f,
+                                C.c_int, C.POINTER(Gradients)]),
+    "pyre_scene_set_materials": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(MaterialDesc), C.c_uint32]),
+    "pyre_scene_set_env": (C.c_int, [C.c_void_p, C.c_void_p, P_f, C.c_float]),
     "pyre_scene_upload_batch": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.c_uint32, C.POINTER(C.c_void_p)]),
     "pyre_render_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(BatchJob), C.c_uint32,
                                     C.POINTER(RenderParams)]),

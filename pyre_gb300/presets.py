@@ -402,3 +402,28 @@ def batch_jobs(n_jobs: int = 256, seed: int = 11, resolutions=(128, 256, 512, 10
                      "spp": int(rng.choice(spps)),
                      "integrator": PathIntegrator(int(rng.integers(depth_range[0], depth_range[1] + 1)), 3)})
     return jobs
+
+
+# ----------------------------------------------------- differentiable render --
+def adjoint_problem(width: int = 512, height: int = 512, env_size=(512, 256), seed: int = 21, n_side: int = 8,
+                    segments: int = 128):
+    """The differentiable-render workload: the procedural studio at width x height
+    with its 64 sphere materials (+ ground) and an env_size FP32 HDRI. Returns
+    (scene, target_scene, camera): the target's parameters are seeded
+    perturbations of the scene's (+-20 % on base color, roughness, metallic,
+    specular, clamped to their ranges; env texels x U[0.5, 2])."""
+    sc = studio_procedural(n_side=n_side, segments=segments, hdri_size=env_size)
+    rng = np.random.default_rng(seed)
+    tgt = Scene(list(sc.primitives), [], list(sc.lights), None)
+    for m in sc.materials:
+        if isinstance(m, DisneyBsdf):
+            f = 1.0 + rng.uniform(-0.2, 0.2, size=6)
+            tgt.materials.append(DisneyBsdf(np.clip(m.base_color * f[:3], 0, 1), float(np.clip(m.metallic * f[3], 0, 1)),
+                                            float(np.clip(m.roughness * f[4], 0.05, 1)),
+                                            float(np.clip(m.specular * f[5], 0, 1))))
+        else:
+            tgt.materials.append(Lambertian(np.clip(m.albedo * (1.0 + rng.uniform(-0.2, 0.2, size=3)), 0, 1)))
+    px = sc.env.pixels * rng.uniform(0.5, 2.0, size=sc.env.pixels.shape).astype(F32)
+    tgt.env = HdriEnvironmentLight(sc.env.width, sc.env.height, px.astype(F32), sc.env.intensity)
+    cam = studio_procedural_camera(width, height)
+    return sc, tgt, cam

@@ -221,6 +221,20 @@ class Film:
 
 
 # ---------------------------------------------------------------- flatten --
+def _material_desc(m) -> N.MaterialDesc:
+    md = N.MaterialDesc()
+    if isinstance(m, Lambertian):
+        md.kind = N.PYRE_MAT_LAMBERTIAN
+        md.base_color[:] = [float(x) for x in m.albedo]
+    elif isinstance(m, DisneyBsdf):
+        md.kind = N.PYRE_MAT_DISNEY
+        md.base_color[:] = [float(x) for x in m.base_color]
+        md.metallic, md.roughness, md.specular = float(m.metallic), float(m.roughness), float(m.specular)
+    else:
+        raise TypeError(f"unsupported material {type(m).__name__}")
+    return md
+
+
 class _Flat:
     """A SceneDesc plus the numpy arrays it points into (kept alive)."""
 
@@ -258,19 +272,7 @@ class _Flat:
                 idd.offset_t0[:] = [float(x) for x in inst.motion.offset_t0]
                 idd.offset_t1[:] = [float(x) for x in inst.motion.offset_t1]
             insts.append(idd)
-        mats = []
-        for m in scene.materials:
-            md = N.MaterialDesc()
-            if isinstance(m, Lambertian):
-                md.kind = N.PYRE_MAT_LAMBERTIAN
-                md.base_color[:] = [float(x) for x in m.albedo]
-            elif isinstance(m, DisneyBsdf):
-                md.kind = N.PYRE_MAT_DISNEY
-                md.base_color[:] = [float(x) for x in m.base_color]
-                md.metallic, md.roughness, md.specular = float(m.metallic), float(m.roughness), float(m.specular)
-            else:
-                raise TypeError(f"unsupported material {type(m).__name__}")
-            mats.append(md)
+        mats = [_material_desc(m) for m in scene.materials]
         lights = []
         for l in scene.lights:
             ld = N.QuadLightDesc()
@@ -425,6 +427,35 @@ class CudaIntegrator:
 
     def set_stage_timing(self, enabled: bool) -> None:
         self.check(self.lib.pyre_set_stage_timing(self.handle, 1 if enabled else 0))
+
+    def backward(self, dscene: DeviceScene, camera: CameraSpec, integrator: PathIntegrator, width: int, height: int,
+                 spp: int, dl_di: np.ndarray, spp_begin: int = 0, crop=None, env_sampling: int = 0,
+                 env_grad: bool = True):
+        """pyre_backward: gradients of a loss with d loss / d film = dl_di (crop h, w, 3).
+
+        Returns (material gradients (n_materials, 6) float64, env gradients (h, w, 3) or None)."""
+        sc = dscene.scene
+        p = self.params(width, height, spp_begin, spp_begin + spp, integrator, crop, env_sampling)
+        mat = np.zeros((len(sc.materials), 6), np.float64)
+        env = np.zeros((sc.env.height, sc.env.width, 3), F32) if (sc.env is not None and env_grad) else None
+        g = N.Gradients(mat.ctypes.data_as(C.POINTER(C.c_double)), N.fptr(env) if env is not None else None,
+                        N.PYRE_MEM_HOST)
+        d = np.ascontiguousarray(dl_di, F32)
+        cam = camera.to_desc()
+        self.check(self.lib.pyre_backward(self.handle, dscene.handle, C.byref(cam), C.byref(p), N.fptr(d),
+                                          N.PYRE_MEM_HOST, C.byref(g)))
+        return mat, env
+
+    def set_materials(self, dscene: DeviceScene, materials: list) -> None:
+        arr = (N.MaterialDesc * max(1, len(materials)))(*[_material_desc(m) for m in materials])
+        self.check(self.lib.pyre_scene_set_materials(self.handle, dscene.handle, arr, len(materials)))
+        dscene.scene.materials = list(materials)
+
+    def set_env(self, dscene: DeviceScene, pixels: np.ndarray, intensity: float = 1.0) -> None:
+        px = np.ascontiguousarray(pixels, F32)
+        self.check(self.lib.pyre_scene_set_env(self.handle, dscene.handle, N.fptr(px), float(intensity)))
+        env = dscene.scene.env
+        dscene.scene.env = HdriEnvironmentLight(env.width, env.height, px, intensity)
 
     def stats(self) -> N.RenderStats:
         s = N.RenderStats()

@@ -1,0 +1,89 @@
+"""Path-replay adjoint vs (1) the oracle's forward-mode dual-number gradient
+(same seeds, same detached convention: cosine >= 0.999) and (2) central
+finite differences with common random numbers."""
+import numpy as np
+import pytest
+
+from pyre_gb300 import presets as P
+from pyre_gb300.native import PYRE_ENV_CDF
+from pyre_gb300.scene import (DisneyBsdf, HdriEnvironmentLight, Lambertian, MeshInstance, PathIntegrator, Primitive,
+                              Scene)
+
+pytestmark = pytest.mark.gpu
+
+
+def cosine(a, b):
+    a, b = np.ravel(a).astype(np.float64), np.ravel(b).astype(np.float64)
+    return float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-300))
+
+
+def small_env_scene():
+    sc = Scene()
+    sc.materials.append(Lambertian([0.55, 0.5, 0.45]))
+    s = 20.0
+    sc.primitives.append(Primitive(MeshInstance.build(
+        P.quad_mesh([(-s, 0, -s), (s, 0, -s), (s, 0, s), (-s, 0, s)], (0, 1, 0))), 0))
+    rng = np.random.default_rng(4)
+    for k, (x, z) in enumerate([(-0.5, 0.0), (0.4, 0.1), (0.0, -0.6)]):
+        sc.materials.append(DisneyBsdf(rng.random(3), float(k == 1), 0.2 + 0.3 * k, 0.5))
+        sc.primitives.append(Primitive(MeshInstance.build(P.make_uv_sphere((x, 0.3, z), 0.3, 24, 12)), k + 1))
+    px = (0.3 + rng.random((8, 16, 3))).astype(np.float32)
+    px[2, 5] = [20.0, 18.0, 14.0]  # a bright texel
+    sc.env = HdriEnvironmentLight(16, 8, px, 1.0)
+    cam = P.studio_ref_camera(48, 48)
+    return sc, cam
+
+
+def test_adjoint_matches_dual_number_oracle(gpu_ctx, oracle_mod):
+    sc, cam = small_env_scene()
+    w = h = 48
+    it = PathIntegrator(6, 3)
+    dl = np.random.default_rng(9).normal(size=(h, w, 3)).astype(np.float32)
+    ds = gpu_ctx.upload(sc)
+    g_mat, g_env = gpu_ctx.backward(ds, cam, it, w, h, 4, dl, env_sampling=PYRE_ENV_CDF)
+    o_mat, o_env = oracle_mod.OracleScene(sc).render_grad(cam, w, h, 4, dl, len(sc.materials), (8, 16),
+                                                          max_depth=6, min_rr_depth=3)
+    cm, ce = cosine(g_mat, o_mat), cosine(g_env, o_env)
+    rel_m = float(np.linalg.norm(g_mat - o_mat) / np.linalg.norm(o_mat))
+    rel_e = float(np.linalg.norm(g_env - o_env) / np.linalg.norm(o_env))
+    print({"cos_materials": cm, "cos_env": ce, "rel_l2_materials": rel_m, "rel_l2_env": rel_e})
+    assert cm >= 0.999 and ce >= 0.999, (cm, ce)
+    assert rel_m < 0.02 and rel_e < 0.02
+    ds.close()
+
+
+def test_adjoint_matches_finite_differences(gpu_ctx):
+    """Lambertian Cornell box, RR off: d loss / d albedo by central differences (common random numbers)."""
+    sc, cam = P.cornell_box(), P.cornell_box_camera(64, 64)
+    w = h = 64
+    it = PathIntegrator(5, 99)  # min_rr_depth beyond max_depth: no Russian roulette
+    spp = 64
+    ds = gpu_ctx.upload(sc)
+    target = gpu_ctx.render(ds, cam, it, w, h, 256, spp_begin=5000).radiance * 0.8
+
+    def loss(img):
+        return float(np.mean((img.astype(np.float64) - target) ** 2))
+
+    img = gpu_ctx.render(ds, cam, it, w, h, spp).radiance
+    dl = (2.0 * (img - target) / img.size).astype(np.float32)
+    g_mat, _ = gpu_ctx.backward(ds, cam, it, w, h, spp, dl)
+    base = list(sc.materials)
+    eps = 1e-3
+    checked = 0
+    for m in range(3):
+        for c in range(3):
+            plus = [Lambertian(x.albedo.copy()) for x in base]
+            minus = [Lambertian(x.albedo.copy()) for x in base]
+            plus[m].albedo[c] += eps
+            minus[m].albedo[c] -= eps
+            gpu_ctx.set_materials(ds, plus)
+            lp = loss(gpu_ctx.render(ds, cam, it, w, h, spp).radiance)
+            gpu_ctx.set_materials(ds, minus)
+            lm = loss(gpu_ctx.render(ds, cam, it, w, h, spp).radiance)
+            fd = (lp - lm) / (2 * eps)
+            ad = g_mat[m, c]
+            assert abs(ad - fd) <= 0.03 * abs(fd) + 1e-7, (m, c, ad, fd)
+            checked += 1
+    gpu_ctx.set_materials(ds, base)
+    assert checked == 9
+    ds.close()
