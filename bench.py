@@ -77,7 +77,7 @@ def run_adjoint(args):
     target = ctx.render(dt, cam, it, w, h, 256, spp_begin=1 << 20).radiance.astype(np.float64)
 
     def step(s0):
-        img = ctx.render(ds, cam, it, w, h, spp, spp_begin=s0).radiance
+        img = ctx.forward(ds, cam, it, w, h, spp, spp_begin=s0).radiance
         f_ms = ctx.stats().ms_total
         dl = (2.0 * (img - target) / img.size).astype(np.float32)
         gm, ge = ctx.backward(ds, cam, it, w, h, spp, dl, spp_begin=s0)

@@ -268,15 +268,25 @@ typedef struct pyre_gradients {
     int mem; /* PYRE_MEM_HOST or PYRE_MEM_DEVICE */
 } pyre_gradients;
 
+/* Forward half of the forward/backward pair: renders exactly like
+ * pyre_render and also keeps each path's final radiance (16 bytes per path
+ * of the sample range) in the context for pyre_backward. */
+int pyre_forward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                 const pyre_render_params* params, pyre_film* film);
+
 /* Path-replay adjoint of pyre_render (no reference counterpart: the
  * reference has no differentiation). Given d loss / d film radiance for the
  * render with the same camera and params (crop-sized, RGB per pixel), it
- * re-traces every path of the sample range from its pixel seed and writes
- * the gradients. Convention: detached sampling; only BSDF values and emitted
- * radiance carry derivatives (pdfs, MIS weights, lobe choice, Russian
- * roulette and the environment's sampling tables are constants), which is
- * unbiased for the derivative of the expected image. Limits: max_depth <= 16,
- * at most 3 quad lights, single (non-batch) scenes. */
+ * replays every path of the sample range from its pixel seed, through the same
+ * wavefront kernels as the forward, and writes the gradients. It uses the
+ * radiance kept by the last pyre_forward with the same scene, camera and
+ * params, or renders it first. Convention: detached sampling; only BSDF
+ * values and emitted radiance carry derivatives (pdfs, MIS weights, lobe
+ * choice, Russian roulette and the environment's sampling tables are
+ * constants), which is unbiased for the derivative of the expected image.
+ * Single (non-batch) scenes only. A colour channel whose BSDF value is
+ * exactly zero at a vertex loses that vertex's BSDF-sample term in that
+ * channel (the replay divides the remaining radiance by f). */
 int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
                   const pyre_render_params* params, const float* d_loss_d_image, int image_mem,
                   pyre_gradients* grads);

@@ -21,7 +21,7 @@ import numpy as np
 def parse(argv=None):
     ap = argparse.ArgumentParser(prog="pyre_gb300.cli")
     ap.add_argument("--preset", default="cornell",
-                    choices=["cornell", "cornell-box", "studio", "studio-procedural", "microbench"])
+                    choices=["cornell", "cornell-box", "studio", "studio-procedural", "microbench", "adjoint"])
     ap.add_argument("--width", type=int, default=800)
     ap.add_argument("--height", type=int, default=600)
     ap.add_argument("--spp", type=int, default=16)
@@ -88,6 +88,27 @@ def microbench(args, ctx) -> int:
     return 0
 
 
+def adjoint(args, ctx) -> int:
+    """One forward render and one path-replay adjoint of the differentiable-render problem."""
+    from . import presets as P
+    from .scene import PathIntegrator
+    sc, tgt, cam = P.adjoint_problem(args.width, args.height, env_size=(512, 256))
+    ds, dt = ctx.upload(sc), ctx.upload(tgt)
+    it = PathIntegrator(args.max_depth, 3)
+    target = ctx.render(dt, cam, it, args.width, args.height, args.spp, spp_begin=1 << 20).radiance
+    for _ in range(args.repeat):
+        img = ctx.forward(ds, cam, it, args.width, args.height, args.spp).radiance
+        f_ms = ctx.stats().ms_total
+        dl = (2.0 * (img - target) / img.size).astype(np.float32)
+        gm, ge = ctx.backward(ds, cam, it, args.width, args.height, args.spp, dl)
+        print(json.dumps({"preset": "adjoint", "forward_ms": f_ms, "adjoint_ms": ctx.stats().ms_total,
+                          "loss": float(np.mean((img - target) ** 2)), "grad_norm_materials": float(np.linalg.norm(gm)),
+                          "grad_norm_env": float(np.linalg.norm(ge))}), flush=True)
+    ds.close()
+    dt.close()
+    return 0
+
+
 def main(argv=None) -> int:
     args = parse(argv)
     from .native import PYRE_ENV_ALIAS, PYRE_ENV_CDF
@@ -95,6 +116,8 @@ def main(argv=None) -> int:
     ctx = CudaIntegrator(0)
     if args.preset == "microbench":
         return microbench(args, ctx)
+    if args.preset == "adjoint":
+        return adjoint(args, ctx)
     scene, cam = _scene(args)
     ds = ctx.upload(scene)
     integ = PathIntegrator(args.max_depth, 3)

@@ -76,7 +76,9 @@ struct D6x3 {
 
 // Value and parameter Jacobian of f(wo, wi) for one material:
 // J[c][k] = d f_c / d param_k.
-__device__ __forceinline__ void bsdf_eval_jac(const Bsdf& b, f3 wo, f3 wi, float J[3][PYRE_NPARAM]) {
+// Not inlined: it is called from several sites of a large kernel, and one
+// out-of-line copy keeps the instruction footprint small.
+static __device__ __noinline__ void bsdf_eval_jac(const Bsdf& b, f3 wo, f3 wi, float J[3][PYRE_NPARAM]) {
 #pragma unroll
     for (int c = 0; c < 3; ++c)
 #pragma unroll
@@ -134,6 +136,41 @@ __device__ __forceinline__ void bsdf_eval_jac(const Bsdf& b, f3 wo, f3 wi, float
     }
 #pragma unroll
     for (int k = 0; k < PYRE_NPARAM; ++k) { J[0][k] = f.x.d[k]; J[1][k] = f.y.d[k]; J[2][k] = f.z.d[k]; }
+}
+
+// The four texels and weights of env_texture's bilinear lookup (light.rs:290-314).
+__device__ __forceinline__ void env_texel_weights(const DevEnv& E, f2 uv, uint32_t idx[4], float wt[4]) {
+    int32_t w = (int32_t)E.width, h = (int32_t)E.height;
+    float u = fract_(fract_(uv.x) + 1.0f);
+    float v = clampf_(uv.y, 0.0f, 1.0f);
+    float fx = u * (float)w - 0.5f;
+    float fy = clampf_(v * (float)h - 0.5f, 0.0f, (float)h - 1.0f);
+    int32_t x0i = sat_i32(floorf(fx)), y0i = sat_i32(floorf(fy));
+    float dx = fx - (float)x0i, dy = fy - (float)y0i;
+    int32_t x0 = ((x0i % w) + w) % w;
+    int32_t x1 = ((x0 + 1) % w + w) % w;
+    int32_t y0 = min(max(y0i, 0), h - 1);
+    int32_t y1 = min(y0 + 1, h - 1);
+    idx[0] = (uint32_t)(y0 * w + x0); wt[0] = (1.0f - dx) * (1.0f - dy);
+    idx[1] = (uint32_t)(y0 * w + x1); wt[1] = dx * (1.0f - dy);
+    idx[2] = (uint32_t)(y1 * w + x0); wt[2] = (1.0f - dx) * dy;
+    idx[3] = (uint32_t)(y1 * w + x1); wt[3] = dx * dy;
+}
+
+// d(loss)/d(texel) for a radiance term c * Le(uv), Le = texture(uv) * intensity.
+__device__ __forceinline__ void scatter_env(const DevEnv& E, float* env_grad, f2 uv, f3 c) {
+    if (!env_grad) return;
+    uint32_t idx[4];
+    float wt[4];
+    env_texel_weights(E, uv, idx, wt);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float s = wt[k] * E.intensity;
+        if (s == 0.0f) continue;
+        atomicAdd(env_grad + 3 * (size_t)idx[k], c.x * s);
+        atomicAdd(env_grad + 3 * (size_t)idx[k] + 1, c.y * s);
+        atomicAdd(env_grad + 3 * (size_t)idx[k] + 2, c.z * s);
+    }
 }
 
 }  // namespace pyre

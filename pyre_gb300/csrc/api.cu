@@ -214,6 +214,7 @@ int pyre_ctx_destroy(pyre_ctx* ctx) {
     if (ctx->wave_graph) cudaGraphExecDestroy(ctx->wave_graph);
     if (ctx->render_ws.ptr) cudaFree(ctx->render_ws.ptr);
     if (ctx->io_ws.ptr) cudaFree(ctx->io_ws.ptr);
+    if (ctx->tape_ws.ptr) cudaFree(ctx->tape_ws.ptr);
     if (ctx->d_error) cudaFree(ctx->d_error);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     for (auto& ev : ctx->ev)

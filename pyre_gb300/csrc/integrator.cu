@@ -24,6 +24,7 @@
 #include <string>
 
 #include "internal.h"
+#include "adjoint.cuh"
 #include "shading.cuh"
 
 namespace cg = cooperative_groups;
@@ -76,7 +77,16 @@ struct WaveParams {
     const DevJob* jobs;
     const DevSeg* segs;
     const DevWave* waves;
+    // adjoint replay
+    const float* dl_di;  // crop npix*3: d loss / d film radiance
+    float inv_spp;
+    double* mat_grad;    // n_mat*6
+    float* env_grad;     // env texels*3 or null
+    uint32_t n_mat;
+    int smem_grad;       // material gradients summed per block in shared memory
 };
+
+#define PYRE_GSLOT 4  // float4s of parked gradient terms per NEE slot
 
 struct PathSoA {
     float4* ray_o;     // origin.xyz
@@ -98,6 +108,10 @@ struct PathSoA {
     float4* acc_n;     // normal sum
     WaveCtl* ctl;
     uint32_t* pjob;    // batch: job of each path
+    // adjoint replay (null otherwise)
+    float4* keep_L;    // per (sample, pixel) of the sample range: final path radiance (pyre_forward)
+    float4* gpend;     // 3 per NEE slot: parked gradient terms of that slot
+    float4* brec;      // 3 per path: BSDF sample of the last vertex (wo+mat, wi+flag, f)
 };
 
 __device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
@@ -284,14 +298,59 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene S, PathSoA P, WaveParam
         if (BATCH && valid) root = W.jobs[P.pjob[target / W.ns]].tlas_root;
         TraceHit h;
         const bool occluded = trace_warp<true>(S, r, valid, root, &h);
-        if (valid && occluded) P.pend[target] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (valid && occluded) {
+            P.pend[target] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (P.gpend) P.gpend[PYRE_GSLOT * (size_t)target + 1].w = 0.0f;  // its gradient terms die with it
+        }
+    }
+}
+
+// ------------------------------------------------------- adjoint helpers --
+// Adds d loss / d (6 parameters of material m), summed per block in shared
+// memory when it fits, else straight into the FP64 gradient.
+__device__ __forceinline__ void add_material_grad(const WaveParams& W, double* sgrad, uint32_t m, const float g[6]) {
+#pragma unroll
+    for (int k = 0; k < PYRE_NPARAM; ++k) {
+        if (g[k] == 0.0f) continue;
+        if (W.smem_grad) atomicAdd(sgrad + PYRE_NPARAM * m + k, (double)g[k]);
+        else atomicAdd(W.mat_grad + PYRE_NPARAM * (size_t)m + k, (double)g[k]);
+    }
+}
+// d loss . (J (x) w): the parameter gradient of a term  w (x) f(wo, wi).
+__device__ __forceinline__ void jac_dot(const Bsdf& b, f3 wo, f3 wi, f3 w, float g[6]) {
+    float J[3][PYRE_NPARAM];
+    bsdf_eval_jac(b, wo, wi, J);
+#pragma unroll
+    for (int k = 0; k < PYRE_NPARAM; ++k) g[k] = w.x * J[0][k] + w.y * J[1][k] + w.z * J[2][k];
+}
+// Applies the parked gradient terms of one visible NEE slot (layout:
+// g0 = params 0-3, g1 = (params 4-5, material bits, pending), g2 = (env uv,
+// env flag, -), g3 = (env texel weight rgb, -)).
+__device__ __forceinline__ void apply_parked_grad(const DevScene& S, const WaveParams& W, double* sgrad,
+                                                  const float4* G) {
+    const float4 g0 = G[0], g1 = G[1];
+    if (g1.w == 0.0f) return;
+    const float g[6] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y};
+    add_material_grad(W, sgrad, __float_as_uint(g1.z), g);
+    const float4 g2 = G[2];
+    if (g2.z != 0.0f) {
+        const float4 g3 = G[3];
+        f2 uv; uv.x = g2.x; uv.y = g2.y;
+        scatter_env(S.env, W.env_grad, uv, mk3(g3.x, g3.y, g3.z));
     }
 }
 
 // ----------------------------------------------------------------- shade --
 // One path vertex of PathIntegrator::integrate (integrator.rs:242-388).
-template <bool BATCH>
+// ADJ: the path-replay adjoint of the same vertex (pyre_backward): the same
+// draws and decisions, plus the derivatives of its terms.
+template <bool BATCH, bool ADJ = false>
 __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+    extern __shared__ double sgrad[];
+    if (ADJ && W.smem_grad) {
+        for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x) sgrad[k] = 0.0;
+        __syncthreads();
+    }
     const uint32_t n = P.ctl->count[depth];
     const uint32_t* qin = P.q[depth & 1];
     uint32_t* qout = P.q[(depth + 1) & 1];
@@ -303,6 +362,13 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
         const uint32_t i = depth == 0 ? j : qin[j];
         float4 Lq = P.L[i];
         f3 L = mk3(Lq.x, Lq.y, Lq.z);
+        f3 delta = splat3(0.0f), Ltot = splat3(0.0f);
+        if (ADJ) {  // adjoint of this path's film pixel, and its forward radiance
+            const uint32_t k = i / W.npix, pp = i - k * W.npix;
+            delta = mk3(W.dl_di[3 * (size_t)pp], W.dl_di[3 * (size_t)pp + 1], W.dl_di[3 * (size_t)pp + 2]) * W.inv_spp;
+            const float4 lt = P.keep_L[(size_t)(P.ctl->s_base - W.spp_begin + k) * W.npix + pp];
+            Ltot = mk3(lt.x, lt.y, lt.z);
+        }
         // Contributions left by the previous vertex's NEE, in light order.
         if (depth > 0) {
             for (uint32_t s = 0; s < W.ns; ++s) {
@@ -310,6 +376,23 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
                 if (c.w != 0.0f) {
                     L = L + mk3(c.x, c.y, c.z);
                     P.pend[(size_t)i * W.ns + s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (ADJ) apply_parked_grad(S, W, sgrad, P.gpend + PYRE_GSLOT * ((size_t)i * W.ns + s));
+                }
+            }
+            if (ADJ) {
+                // BSDF sample of the previous vertex: beta_d * a * R_{d+1} = (L_total - L_so_far) / f
+                const float4 b0 = P.brec[3 * (size_t)i], b1 = P.brec[3 * (size_t)i + 1], b2 = P.brec[3 * (size_t)i + 2];
+                if (b1.w != 0.0f) {
+                    const f3 after = Ltot - L;
+                    const f3 w = mk3(b2.x > 0.0f ? delta.x * after.x / b2.x : 0.0f,
+                                     b2.y > 0.0f ? delta.y * after.y / b2.y : 0.0f,
+                                     b2.z > 0.0f ? delta.z * after.z / b2.z : 0.0f);
+                    if (!is_zero3(w)) {
+                        const uint32_t m = __float_as_uint(b0.w);
+                        float g[6];
+                        jac_dot(load_bsdf(S, m), mk3(b0.x, b0.y, b0.z), mk3(b1.x, b1.y, b1.z), w, g);
+                        add_material_grad(W, sgrad, m, g);
+                    }
                 }
             }
         }
@@ -328,12 +411,16 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
             if (S.has_env) {
                 f3 le = env_le(S.env, ray_d);
                 if (!is_zero3(le)) {
+                    float w_adj = 1.0f;
                     if (last_was_specular) L = L + beta * le;
                     else {
                         float pdf_env = env_pdf(S.env, ray_d);
                         float w = power_heuristic(last_pdf, pdf_env);
                         L = L + beta * le * w;
+                        w_adj = w;
                     }
+                    // d/d texels of beta * texture(uv) * intensity * w
+                    if (ADJ) scatter_env(S.env, W.env_grad, env_dir_to_uv(ray_d), delta * beta * w_adj);
                 }
             }
         } else if (code <= -2) {
@@ -412,6 +499,14 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
                     f3 contrib = beta * f * Lt.emission * wi.z * w / lpdf;
                     size_t sidx = (size_t)i * W.ns + l;
                     P.pend[sidx] = make_float4(contrib.x, contrib.y, contrib.z, 1.0f);
+                    if (ADJ) {  // park d/d params of beta * f * (Le cos w / pdf); cleared if occluded
+                        float gm[6];
+                        jac_dot(mat, wo, wi, delta * beta * (Lt.emission * wi.z * w / lpdf), gm);
+                        float4* G = P.gpend + PYRE_GSLOT * sidx;
+                        G[0] = make_float4(gm[0], gm[1], gm[2], gm[3]);
+                        G[1] = make_float4(gm[4], gm[5], __uint_as_float(I.material), 1.0f);
+                        G[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    }
                     if (dist > 0.0f) {
                         f3 dir = tf / dist;
                         P.sh_o[sidx] = make_float4(p_off.x, p_off.y, p_off.z, dist - 1e-3f);
@@ -435,6 +530,18 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
                                 f3 contrib = beta * f * eli * wi.z * w / epdf;
                                 size_t sidx = (size_t)i * W.ns + S.n_lights;
                                 P.pend[sidx] = make_float4(contrib.x, contrib.y, contrib.z, 1.0f);
+                                if (ADJ) {  // term beta * f * (texture * intensity) * k, k = cos w / pdf
+                                    const float k = wi.z * w / epdf;
+                                    float gm[6];
+                                    jac_dot(mat, wo, wi, delta * beta * (eli * k), gm);
+                                    const f2 uv = env_dir_to_uv(ewi);
+                                    const f3 ke = delta * beta * f * k;
+                                    float4* G = P.gpend + PYRE_GSLOT * sidx;
+                                    G[0] = make_float4(gm[0], gm[1], gm[2], gm[3]);
+                                    G[1] = make_float4(gm[4], gm[5], __uint_as_float(I.material), 1.0f);
+                                    G[2] = make_float4(uv.x, uv.y, 1.0f, 0.0f);
+                                    G[3] = make_float4(ke.x, ke.y, ke.z, 0.0f);
+                                }
                                 P.sh_o[sidx] = make_float4(p_off.x, p_off.y, p_off.z, INF);
                                 P.sh_d[sidx] = make_float4(ewi.x, ewi.y, ewi.z, time);
                                 P.sq[append_slot(shadow_count)] = (uint32_t)sidx;
@@ -462,6 +569,11 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
                             P.ray_d[i] = make_float4(nd.x, nd.y, nd.z, time);
                             P.beta[i] = make_float4(beta.x, beta.y, beta.z, bpdf);
                             alive = true;
+                            if (ADJ) {  // for the next vertex's BSDF-sample gradient
+                                P.brec[3 * (size_t)i] = make_float4(wo.x, wo.y, wo.z, __uint_as_float(I.material));
+                                P.brec[3 * (size_t)i + 1] = make_float4(bwi.x, bwi.y, bwi.z, 1.0f);
+                                P.brec[3 * (size_t)i + 2] = make_float4(bf.x, bf.y, bf.z, 0.0f);
+                            }
                         }
                     }
                 }
@@ -471,6 +583,30 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
         P.L[i] = make_float4(L.x, L.y, L.z, 0.0f);
         if (alive && depth + 1 < (BATCH ? W.jobs[P.pjob[i]].max_depth : W.max_depth))
             qout[append_slot(next_count)] = i;
+    }
+    if (ADJ && W.smem_grad) {  // one FP64 atomic per parameter per block
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x)
+            if (sgrad[k] != 0.0) atomicAdd(W.mat_grad + k, sgrad[k]);
+    }
+}
+
+// Adjoint replay: parked gradient terms of the paths' last vertices.
+__global__ void k_accumulate_adjoint(DevScene S, PathSoA P, WaveParams W) {
+    extern __shared__ double sgrad[];
+    if (W.smem_grad) {
+        for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x) sgrad[k] = 0.0;
+        __syncthreads();
+    }
+    const uint32_t n = P.ctl->n_valid;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (uint32_t s = 0; s < W.ns; ++s)
+            if (P.pend[(size_t)i * W.ns + s].w != 0.0f)
+                apply_parked_grad(S, W, sgrad, P.gpend + PYRE_GSLOT * ((size_t)i * W.ns + s));
+    if (W.smem_grad) {
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x)
+            if (sgrad[k] != 0.0) atomicAdd(W.mat_grad + k, sgrad[k]);
     }
 }
 
@@ -493,6 +629,8 @@ __global__ void k_accumulate(PathSoA P, WaveParams W) {
             ar.x += L.x; ar.y += L.y; ar.z += L.z; ar.w += a.w;
             aa.x += a.x; aa.y += a.y; aa.z += a.z;
             an.x += nn.x; an.y += nn.y; an.z += nn.z;
+            if (P.keep_L)  // pyre_forward: the path's radiance, for the adjoint replay
+                P.keep_L[(size_t)(P.ctl->s_base - W.spp_begin + k) * W.npix + p] = make_float4(L.x, L.y, L.z, 0.0f);
         }
         P.acc_r[p] = ar; P.acc_a[p] = aa; P.acc_n[p] = an;
     }
@@ -628,7 +766,8 @@ struct Carver {
     }
 };
 
-size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* out, bool batch = false) {
+size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* out, bool batch = false,
+                   bool adjoint = false) {
     Carver c{base};
     PathSoA s;
     s.ray_o = c.take<float4>(P);
@@ -651,6 +790,9 @@ size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* ou
     s.acc_n = c.take<float4>(npix);
     s.ctl = c.take<WaveCtl>(1);
     s.pjob = batch ? c.take<uint32_t>(P) : nullptr;
+    s.keep_L = nullptr;
+    s.gpend = adjoint ? c.take<float4>(P * ns * PYRE_GSLOT) : nullptr;
+    s.brec = adjoint ? c.take<float4>(3 * P) : nullptr;
     if (out) *out = s;
     return c.off + 256;
 }
@@ -747,10 +889,22 @@ uint32_t kernels_per_wave(const WaveParams& W) { return 4 + W.max_depth * (W.ns 
 
 using namespace pyre;
 
+static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                       const pyre_render_params* params, pyre_film* film, float4* keep);
+
 extern "C" {
 
 int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
                 const pyre_render_params* params, pyre_film* film) {
+    return render_impl(ctx, scene, camera, params, film, nullptr);
+}
+
+}  // extern "C"
+
+// The render; with `keep` non-null each path's final radiance is also
+// written to keep[(s - spp_begin) * npix + pixel] (pyre_forward).
+static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                       const pyre_render_params* params, pyre_film* film, float4* keep) {
     if (!ctx || !scene || !camera || !params || !film)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_render: NULL argument");
     cudaSetDevice(ctx->device);
@@ -791,6 +945,7 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
     if (rc) return rc;
     PathSoA S;
     carve_paths((char*)ctx->render_ws.ptr, P, std::max(W.ns, 1u), W.npix, &S);
+    S.keep_L = keep;
     if (film->mem == PYRE_MEM_HOST && (rc = ensure_workspace(ctx, ctx->io_ws, film_bytes))) return rc;
 
     const Launch Lc = make_launch<false>(ctx, rp.block_size);
@@ -804,7 +959,7 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
 
     const DevScene& D = scene->dev;
     ctx->stage_used = 0;
-    if (rp.use_graph && !ctx->stage_timing) {
+    if (rp.use_graph && !ctx->stage_timing && !keep) {
         // One wave captured once per configuration, replayed `waves` times.
         char key[256];
         std::snprintf(key, sizeof key, "%llu/%p/%u/%u/%u/%u/%u/%u/%u/%u/%d", (unsigned long long)scene->serial, ctx->render_ws.ptr,
@@ -874,8 +1029,6 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
     }
     return PYRE_OK;
 }
-
-}  // extern "C"
 
 // ----------------------------------------------------------- batch render --
 extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const pyre_batch_job* jobs,
@@ -1239,3 +1392,166 @@ int pyre_intersect_any(pyre_ctx* ctx, const pyre_scene* scene, const pyre_rays* 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------- forward / backward --
+// Path-replay adjoint (no reference counterpart: the reference has no
+// differentiation). pyre_forward renders like pyre_render and keeps every
+// path's final radiance L_total in the context. pyre_backward replays the
+// same waves (same kernels, seeds, draws and decisions; k_shade<false, true>
+// adds the derivatives) under the detached-sampling convention: only BSDF
+// values and emitted radiance carry derivatives. NEE and emission terms are
+// differentiated where they arise (NEE ones parked with the radiance and
+// dropped by the shadow stage when occluded); the BSDF-sample term of vertex
+// d uses beta_{d+1} * R_{d+1} = L_total - L_so_far, exact because the replay
+// sums contributions in the forward's order.
+namespace {
+std::string tape_key(const pyre_scene* scene, const pyre_camera_desc* camera, const pyre_render_params& rp) {
+    std::string k = std::to_string(scene->serial) + "/";
+    k.append(reinterpret_cast<const char*>(camera), sizeof *camera);
+    const uint32_t f[] = {rp.width, rp.height, rp.spp_begin, rp.spp_end, rp.max_depth, rp.min_rr_depth,
+                          rp.crop[0], rp.crop[1], rp.crop[2], rp.crop[3], rp.env_sampling};
+    k.append(reinterpret_cast<const char*>(f), sizeof f);
+    return k;
+}
+uint64_t crop_pixels(const pyre_render_params& rp) {
+    uint32_t x0 = rp.crop[0], y0 = rp.crop[1], x1 = rp.crop[2], y1 = rp.crop[3];
+    if (x0 == 0 && y0 == 0 && x1 == 0 && y1 == 0) { x1 = rp.width; y1 = rp.height; }
+    return (x1 > x0 && y1 > y0) ? (uint64_t)(x1 - x0) * (y1 - y0) : 0;
+}
+int forward_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                 const pyre_render_params* params, pyre_film* film) {
+    const pyre_render_params& rp = *params;
+    const uint64_t paths = crop_pixels(rp) * (rp.spp_end > rp.spp_begin ? rp.spp_end - rp.spp_begin : 0);
+    int rc = ensure_workspace(ctx, ctx->tape_ws, std::max<uint64_t>(paths, 1) * sizeof(float4));
+    if (rc) return rc;
+    ctx->tape_key.clear();
+    rc = render_impl(ctx, scene, camera, params, film, (float4*)ctx->tape_ws.ptr);
+    if (rc == PYRE_OK) ctx->tape_key = tape_key(scene, camera, rp);
+    return rc;
+}
+}  // namespace
+
+extern "C" int pyre_forward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                            const pyre_render_params* params, pyre_film* film) {
+    if (!ctx || !scene || !camera || !params || !film)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_forward: NULL argument");
+    return forward_impl(ctx, scene, camera, params, film);
+}
+
+extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                             const pyre_render_params* params, const float* d_loss_d_image, int image_mem,
+                             pyre_gradients* grads) {
+    if (!ctx || !scene || !camera || !params || !d_loss_d_image || !grads)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_backward: NULL argument");
+    PYRE_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const pyre_render_params& rp = *params;
+    if (rp.width == 0 || rp.height == 0) return set_error(ctx, PYRE_ERR_INVALID, "image size is zero");
+    if (rp.spp_end <= rp.spp_begin) return set_error(ctx, PYRE_ERR_INVALID, "empty sample range");
+    if (rp.max_depth > PYRE_MAX_DEPTH) return set_error(ctx, PYRE_ERR_INVALID, "max_depth above 64");
+    if (scene->n_parts != 1) return set_error(ctx, PYRE_ERR_UNSUPPORTED, "pyre_backward: batched scenes");
+    if (camera->kind > PYRE_CAMERA_THIN_LENS) return set_error(ctx, PYRE_ERR_INVALID, "unknown camera kind");
+    if (image_mem != PYRE_MEM_HOST && image_mem != PYRE_MEM_DEVICE)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_backward: bad image_mem");
+    if (grads->mem != PYRE_MEM_HOST && grads->mem != PYRE_MEM_DEVICE)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_backward: bad grads.mem");
+    uint32_t x0 = rp.crop[0], y0 = rp.crop[1], x1 = rp.crop[2], y1 = rp.crop[3];
+    if (x0 == 0 && y0 == 0 && x1 == 0 && y1 == 0) { x1 = rp.width; y1 = rp.height; }
+    if (x1 > rp.width || y1 > rp.height || x0 >= x1 || y0 >= y1)
+        return set_error(ctx, PYRE_ERR_INVALID, "crop outside the image");
+    int rc;
+    // L_total of every path: kept by pyre_forward with the same arguments, or recomputed now
+    if (ctx->tape_key != tape_key(scene, camera, rp)) {
+        pyre_film none;
+        std::memset(&none, 0, sizeof none);
+        none.mem = PYRE_MEM_DEVICE;
+        if ((rc = forward_impl(ctx, scene, camera, params, &none))) return rc;
+    }
+
+    WaveParams W;
+    std::memset(&W, 0, sizeof W);
+    W.cam = make_camera(*camera);
+    W.width = rp.width; W.height = rp.height;
+    W.cx0 = x0; W.cy0 = y0; W.cw = x1 - x0; W.ch = y1 - y0;
+    W.npix = W.cw * W.ch;
+    W.spp_begin = rp.spp_begin; W.spp_end = rp.spp_end;
+    W.max_depth = rp.max_depth; W.min_rr = rp.min_rr_depth;
+    W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
+    W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
+    const uint32_t spp = rp.spp_end - rp.spp_begin;
+    uint64_t K = std::max<uint64_t>(1, (rp.wave_paths ? rp.wave_paths : (uint64_t)8 << 20) / W.npix);
+    K = std::min<uint64_t>(K, spp);
+    if ((uint64_t)W.npix * K > (uint64_t)1 << 31) K = std::max<uint64_t>(1, ((uint64_t)1 << 31) / W.npix);
+    W.k_per_wave = (uint32_t)K;
+    const size_t P = (size_t)W.npix * K;
+    const uint32_t waves = (uint32_t)((spp + K - 1) / K);
+
+    const uint32_t n_mat = scene->dev.n_materials;
+    const size_t mat_bytes = (size_t)n_mat * PYRE_NPARAM * sizeof(double);
+    const size_t env_elems = scene->dev.has_env ? (size_t)scene->dev.env.width * scene->dev.env.height * 3 : 0;
+    const size_t img_bytes = (size_t)W.npix * 3 * sizeof(float);
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t path_bytes = carve_paths(nullptr, P, std::max(W.ns, 1u), W.npix, nullptr, false, true);
+    if ((rc = ensure_workspace(ctx, ctx->render_ws, path_bytes))) return rc;
+    if ((rc = ensure_workspace(ctx, ctx->io_ws, al(mat_bytes) + al(env_elems * 4) + al(img_bytes) + 256))) return rc;
+    PathSoA S;
+    carve_paths((char*)ctx->render_ws.ptr, P, std::max(W.ns, 1u), W.npix, &S, false, true);
+    S.keep_L = (float4*)ctx->tape_ws.ptr;
+    char* b = (char*)ctx->io_ws.ptr;
+    double* d_mat = grads->mem == PYRE_MEM_DEVICE && grads->materials ? grads->materials : (double*)b;
+    float* d_env = grads->mem == PYRE_MEM_DEVICE && grads->env ? grads->env : (float*)(b + al(mat_bytes));
+    const float* d_img = d_loss_d_image;
+    cudaStream_t st = ctx->stream;
+    if (image_mem == PYRE_MEM_HOST) {
+        float* tmp = (float*)(b + al(mat_bytes) + al(env_elems * 4));
+        PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(tmp, d_loss_d_image, img_bytes, cudaMemcpyHostToDevice, st));
+        d_img = tmp;
+    }
+    if (mat_bytes) PYRE_CUDA_TRY(ctx, cudaMemsetAsync(d_mat, 0, mat_bytes, st));
+    if (env_elems && grads->env) PYRE_CUDA_TRY(ctx, cudaMemsetAsync(d_env, 0, env_elems * 4, st));
+    W.dl_di = d_img;
+    W.inv_spp = 1.0f / (float)spp;
+    W.mat_grad = d_mat;
+    W.env_grad = (env_elems && grads->env) ? d_env : nullptr;
+    W.n_mat = n_mat;
+    const size_t smem = mat_bytes <= 48 * 1024 ? mat_bytes : 0;
+    W.smem_grad = smem ? 1 : 0;
+
+    const Launch Lc = make_launch<false>(ctx, rp.block_size);
+    const int grid_adj = grid_for(ctx, k_shade<false, true>, Lc.block_shade, smem);
+    const int grid_acc = grid_for(ctx, k_accumulate_adjoint, Lc.block_shade, smem);
+    PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
+    const DevScene& D = scene->dev;
+    for (uint32_t w = 0; w < waves; ++w) {
+        k_wave_begin<<<1, 32, 0, st>>>(S.ctl, W.spp_begin, W.spp_end, W.k_per_wave, W.npix);
+        k_raygen<false><<<Lc.grid_raygen, Lc.block_shade, 0, st>>>(S, W);
+        for (uint32_t d = 0; d < W.max_depth; ++d) {
+            k_extend<false><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(D, S, W, d);
+            k_shade<false, true><<<grid_adj, Lc.block_shade, smem, st>>>(D, S, W, d);
+            if (W.ns > 0) k_shadow<false><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(D, S, W, d);
+        }
+        k_accumulate_adjoint<<<grid_acc, Lc.block_shade, smem, st>>>(D, S, W);
+        k_wave_end<<<1, 32, 0, st>>>(S.ctl, W.max_depth);
+    }
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[1], st));
+    if (grads->mem == PYRE_MEM_HOST) {
+        if (grads->materials && mat_bytes)
+            PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(grads->materials, d_mat, mat_bytes, cudaMemcpyDeviceToHost, st));
+        if (grads->env && env_elems)
+            PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(grads->env, d_env, env_elems * 4, cudaMemcpyDeviceToHost, st));
+    }
+    WaveCtl ctl;
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(&ctl, S.ctl, sizeof ctl, cudaMemcpyDeviceToHost, st));
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    if ((rc = take_kernel_error(ctx))) return rc;
+    pyre_render_stats& s = ctx->stats;
+    std::memset(&s, 0, sizeof s);
+    s.samples = ctl.samples;
+    s.extend_rays = ctl.extend_rays;
+    s.shadow_rays = ctl.shadow_rays;
+    s.waves = waves;
+    s.kernel_launches = waves * kernels_per_wave(W);
+    cudaEventElapsedTime(&s.ms_total, ctx->ev[0], ctx->ev[1]);
+    return PYRE_OK;
+}

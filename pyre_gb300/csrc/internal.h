@@ -35,6 +35,8 @@ struct pyre_ctx {
     unsigned int* d_counter = nullptr;  // work counter of the intersect kernels
     Workspace render_ws;        // path state of the wavefront integrator
     Workspace io_ws;            // staging for host-memory rays / films
+    Workspace tape_ws;          // pyre_forward: per-path radiance for pyre_backward
+    std::string tape_key;       // the render that tape_ws holds
     pyre_render_stats stats{};
     int stage_timing = 0;
     cudaEvent_t ev[16] = {};

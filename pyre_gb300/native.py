@@ -142,6 +142,7 @@ SIGNATURES = {
     "pyre_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams),
                                       C.POINTER(Film)]),
     "pyre_set_stage_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "pyre_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams), C.POINTER(Film)]),
     "pyre_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams), P_f,
                                 C.c_int, C.POINTER(Gradients)]),
     "pyre_scene_set_materials": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(MaterialDesc), C.c_uint32]),

@@ -428,6 +428,17 @@ class CudaIntegrator:
     def set_stage_timing(self, enabled: bool) -> None:
         self.check(self.lib.pyre_set_stage_timing(self.handle, 1 if enabled else 0))
 
+    def forward(self, dscene: DeviceScene, camera: CameraSpec, integrator: PathIntegrator, width: int, height: int,
+                spp: int, spp_begin: int = 0, crop=None, env_sampling: int = 0) -> Film:
+        """pyre_forward: render() that also keeps per-path radiance for backward()."""
+        x0, y0, x1, y1 = crop if crop is not None else (0, 0, width, height)
+        film = Film(x1 - x0, y1 - y0)
+        f = N.Film(N.fptr(film.radiance), N.fptr(film.albedo), N.fptr(film.normal), N.fptr(film.depth), N.PYRE_MEM_HOST)
+        cam = camera.to_desc()
+        p = self.params(width, height, spp_begin, spp_begin + spp, integrator, crop, env_sampling)
+        self.check(self.lib.pyre_forward(self.handle, dscene.handle, C.byref(cam), C.byref(p), C.byref(f)))
+        return film
+
     def backward(self, dscene: DeviceScene, camera: CameraSpec, integrator: PathIntegrator, width: int, height: int,
                  spp: int, dl_di: np.ndarray, spp_begin: int = 0, crop=None, env_sampling: int = 0,
                  env_grad: bool = True):

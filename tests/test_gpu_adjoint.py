@@ -87,3 +87,20 @@ def test_adjoint_matches_finite_differences(gpu_ctx):
     gpu_ctx.set_materials(ds, base)
     assert checked == 9
     ds.close()
+
+
+def test_backward_uses_forward_tape(gpu_ctx):
+    """backward() after forward() (kept radiance) equals backward() that re-renders it."""
+    sc, cam = small_env_scene()
+    it = PathIntegrator(6, 3)
+    dl = np.random.default_rng(2).normal(size=(48, 48, 3)).astype(np.float32)
+    ds = gpu_ctx.upload(sc)
+    a_m, a_e = gpu_ctx.backward(ds, cam, it, 48, 48, 4, dl, env_sampling=PYRE_ENV_CDF, spp_begin=7)
+    film = gpu_ctx.forward(ds, cam, it, 48, 48, 4, env_sampling=PYRE_ENV_CDF, spp_begin=7)
+    ref = gpu_ctx.render(ds, cam, it, 48, 48, 4, env_sampling=PYRE_ENV_CDF, spp_begin=7)
+    np.testing.assert_array_equal(film.radiance, ref.radiance)
+    b_m, b_e = gpu_ctx.backward(ds, cam, it, 48, 48, 4, dl, env_sampling=PYRE_ENV_CDF, spp_begin=7)
+    np.testing.assert_allclose(a_m, b_m, rtol=1e-9, atol=1e-12)
+    # Texel gradients sum by FP32 atomics whose order varies run to run.
+    np.testing.assert_allclose(a_e, b_e, rtol=0, atol=1e-5 * float(np.abs(b_e).max()))
+    ds.close()
