@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=0, help="rows in the CPU sample (0 = auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--graph", type=int, default=0, help="replay waves through a CUDA graph")
+    ap.add_argument("--refill", type=int, default=0,
+                    help="traversal: idle lanes of a warp that trigger a ray refetch (0 = library default)")
     ap.add_argument("--workload", default="studio", choices=["studio", "batch", "adjoint"],
                     help="studio: the 1080p headline frame; batch: 256 Cornell-variant jobs in one batched launch")
     ap.add_argument("--jobs", type=int, default=256, help="batch workload: number of jobs")
@@ -147,7 +149,8 @@ def run_batch(args):
              "integrator": j["integrator"]} for k, j in enumerate(jobs)]
     samples = sum(j["width"] * j["height"] * j["spp"] for j in jobs)
     best, trials = autotune.tune_batch(ctx, ds, spec)
-    knobs = dict(wave_paths=best["wave_paths"], use_graph=best["use_graph"], block_size=best["block_size"])
+    knobs = dict(wave_paths=best["wave_paths"], use_graph=best["use_graph"], block_size=best["block_size"],
+                 sort_by_material=best.get("sort_by_material", 0), refill_lanes=best.get("refill_lanes", 0))
     for _ in range(args.warmup):
         ctx.render_batch(ds, spec, **knobs)
     batch_ms = []
@@ -324,7 +327,8 @@ def main():
     integ = PathIntegrator(DEPTH, RR)
     # Weak scaling: rank r renders samples [r*64, (r+1)*64) of the frame.
     s0 = rank * SPP
-    params = CudaIntegrator.params(W, H, s0, s0 + SPP, integ, env_sampling=N.PYRE_ENV_ALIAS, use_graph=args.graph)
+    params = CudaIntegrator.params(W, H, s0, s0 + SPP, integ, env_sampling=N.PYRE_ENV_ALIAS, use_graph=args.graph,
+                                    refill_lanes=args.refill)
     npix = W * H
     dev = {k: torch.empty(npix * c, dtype=torch.float32, device="cuda") for k, c in
            (("radiance", 3), ("albedo", 3), ("normal", 3), ("depth", 1))}
@@ -414,7 +418,8 @@ def main():
                        "global_batch": world, "seq_len": None, "parallelism": f"replicas x{world} (spp ranges)",
                        "l2": "inputs larger than L2 (scene %.0f MB + path state)" % (info.device_bytes / 1e6),
                        "triangles": int(info.n_triangles), "scene_gen_s": round(gen_s, 2),
-                       "scene_upload_s": round(upload_s, 2), "use_graph": args.graph},
+                       "scene_upload_s": round(upload_s, 2), "use_graph": args.graph,
+                       "refill_lanes": args.refill},
             "mrays_per_s": (ext_rays + shadow_rays) * world / t_max / 1e6,
             "rays": {"extend": ext_rays // args.steps, "shadow": shadow_rays // args.steps},
             "wall_s_timed": wall,

@@ -223,7 +223,9 @@ typedef struct pyre_render_params {
     uint32_t block_size;             /* threads per block of the stage kernels; 0 = 256 */
     uint32_t sort_by_material;       /* reorder the shade queue by material */
     uint32_t use_graph;              /* capture one wave as a CUDA graph and replay it */
-    uint32_t reserved[4];
+    uint32_t refill_lanes;           /* traversal: refetch rays once this many lanes of a
+                                        warp are idle (1-32); 0 = 16 */
+    uint32_t reserved[3];
 } pyre_render_params;
 
 /* Film: per-pixel means over the sample range (PixelSample fields,

@@ -134,8 +134,14 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 // Scene::intersect / Scene::occluded (scene.rs:57-140): closest hit with the
 // canonical tie rule, or any hit.
 //
-// All 32 lanes of the warp must call it (lanes without a ray pass
-// valid = false). Each lane keeps one tagged stack:
+// trace_stream is a persistent loop for one warp over a queue of n rays: the
+// lanes take rays from the queue through a shared work counter, and whenever
+// at least `refill` lanes have finished their ray (or the warp has none), the
+// idle lanes take new rays with one atomic for the warp, so the warp does not
+// run on with a few long rays. A ray's traversal does not depend on which
+// lane or warp runs it, so the results are the same as one ray per thread.
+//
+// Each lane keeps one tagged stack:
 //   [0, 2^29)          node of an instance BVH
 //   TOP | n            node of the top-level BVH
 //   INST | slot        enter instance `slot` (root-box test, local origin)
@@ -144,30 +150,42 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 // lane that already holds one leaf keeps stepping speculatively. Leaves found
 // on the way are parked (at most three triangle ranges, all of the current
 // instance: a lane holding leaves does not leave or enter an instance) and
-// then tested by all lanes in lock step. An any-hit lane is marked finished
-// rather than returning, so lanes stay converged.
+// then tested by all lanes in lock step. An any-hit lane that finds a hit is
+// finished at the end of that leaf phase.
+//
+// Src supplies the rays and takes the results:
+//   uint32_t load(uint32_t j, TraceRay& r, int32_t& root)  ray j of the queue,
+//            the top-level root to trace; returns the id passed to store
+//   void store(uint32_t id, const TraceRay& r, TraceHit& h, bool found)
+// All 32 lanes of the warp must call trace_stream with the same n and counter.
 #define PYRE_TAG_TOP (1 << 29)
 #define PYRE_TAG_INST (1 << 30)
 #define PYRE_NODE_NONE (-1)
 #define PYRE_NODE_EXIT (-2)
 
-template <bool ANY>
-__device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r, bool valid, int32_t root,
-                                           TraceHit* hit) {
+template <bool ANY, class Src>
+__device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, uint32_t n, uint32_t* counter,
+                                             int refill) {
     const unsigned FULL = 0xffffffffu;
-    hit->inst = -1; hit->tri = -1; hit->light = -1;
-    hit->t = r.tmax; hit->u = 0.0f; hit->v = 0.0f;
-    const f3 inv = mk3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
-    float best_t = r.tmax;
+    const int lane = threadIdx.x & 31;
+    const unsigned lanes_below = (1u << lane) - 1u;
+    bool drained = false;   // warp-uniform: the queue has no rays left
+    bool active = false;    // the lane holds a ray
+    uint32_t id = 0;
+    TraceRay r;
+    r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.tmin = 0.0f; r.tmax = 0.0f; r.time = 0.0f;
+    TraceHit hit;
+    hit.inst = -1; hit.tri = -1; hit.light = -1; hit.t = 0.0f; hit.u = 0.0f; hit.v = 0.0f;
+    f3 inv = splat3(0.0f);
+    float best_t = 0.0f;
     uint32_t best_key = 0xffffffffu;
     int32_t best_orig = 0x7fffffff;
     bool found = false;
-    // term: the lane has nothing left to do; exhausted: no node left to step
-    bool term = !valid || root < 0;
-    bool exhausted = term;
+    bool hit_any = false;    // any-hit: the ray is occluded
+    bool exhausted = true;   // no node left to step
     int stack[PYRE_STACK];
     int sp = 0;
-    int node = term ? PYRE_NODE_NONE : (root | PYRE_TAG_TOP);
+    int node = PYRE_NODE_NONE;
     int inst = -1;
     int32_t inst_orig = 0;
     f3 o = r.o;
@@ -176,10 +194,48 @@ __device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r,
     int ls[3] = {0, 0, 0}, lc[3] = {0, 0, 0};
     int parked = 0;
 
-    while (__any_sync(FULL, !term)) {
+    while (true) {
+        // ---- refill idle lanes from the queue
+        if (!drained) {
+            const unsigned idle = __ballot_sync(FULL, !active);
+            const int n_idle = __popc(idle);
+            if (n_idle >= refill || n_idle == 32) {
+                const int leader = __ffs(idle) - 1;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(counter, (uint32_t)n_idle);
+                base = __shfl_sync(FULL, base, leader);
+                if ((uint64_t)base + (uint64_t)n_idle >= (uint64_t)n) drained = true;
+                const uint32_t j = base + (uint32_t)__popc(idle & lanes_below);
+                if (!active && j < n) {
+                    int32_t root;
+                    id = src.load(j, r, root);
+                    active = true;
+                    inv = mk3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
+                    hit.inst = -1; hit.tri = -1; hit.light = -1;
+                    hit.t = r.tmax; hit.u = 0.0f; hit.v = 0.0f;
+                    best_t = r.tmax;
+                    best_key = 0xffffffffu;
+                    best_orig = 0x7fffffff;
+                    found = false;
+                    hit_any = false;
+                    exhausted = root < 0;
+                    sp = 0;
+                    node = exhausted ? PYRE_NODE_NONE : (root | PYRE_TAG_TOP);
+                    inst = -1;
+                    inst_orig = 0;
+                    o = r.o;
+                    parked = 0;
+                    lc[0] = lc[1] = lc[2] = 0;
+                }
+            }
+        }
+        if (!__any_sync(FULL, active)) {
+            if (drained) break;
+            continue;
+        }
         // ---- inner phase: step nodes until every lane holds a leaf or has none left
-        while (__any_sync(FULL, !term && !exhausted && parked == 0)) {
-            if (term || exhausted || parked >= 2) continue;
+        while (__any_sync(FULL, active && !exhausted && !hit_any && parked == 0)) {
+            if (!active || exhausted || hit_any || parked >= 2) continue;
             if (node == PYRE_NODE_NONE) {
                 if (sp == 0) { exhausted = true; continue; }
                 node = stack[--sp];
@@ -205,7 +261,7 @@ __device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r,
                 }
                 float e;
                 if (!slab(I.lo[0], I.hi[0], I.lo[1], I.hi[1], I.lo[2], I.hi[2], lo, inv, r.tmin, best_t, &e)) continue;
-                if (sp >= PYRE_STACK) { atomicExch(S.error_flag, -5); term = exhausted = true; continue; }
+                if (sp >= PYRE_STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                 stack[sp++] = PYRE_NODE_EXIT;
                 inst = k;
                 inst_orig = I.orig_id;
@@ -225,7 +281,7 @@ __device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r,
             // leaves: park triangle ranges, or queue the instances of a top-level leaf
             if (top) {
                 const int need = (h0 && leaf0 ? nd.z : 0) + (h1 && leaf1 ? nd.w : 0) + 1;
-                if (sp + need > PYRE_STACK) { atomicExch(S.error_flag, -5); term = exhausted = true; continue; }
+                if (sp + need > PYRE_STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                 if (h1 && leaf1)
                     for (int k = nd.w - 1; k >= 0; --k) stack[sp++] = PYRE_TAG_INST | (nd.y + k);
                 if (h0 && leaf0)
@@ -238,7 +294,7 @@ __device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r,
             const bool g0 = h0 && !leaf0, g1 = h1 && !leaf1;
             if (g0 && g1) {
                 const bool first0 = e0 <= e1;
-                if (sp >= PYRE_STACK) { atomicExch(S.error_flag, -5); term = exhausted = true; continue; }
+                if (sp >= PYRE_STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                 stack[sp++] = (first0 ? nd.y : nd.x) | tag;
                 node = (first0 ? nd.x : nd.y) | tag;
             } else if (g0) {
@@ -248,18 +304,19 @@ __device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r,
             }
         }
         // ---- leaf phase: all lanes test their parked triangles together
-        const int c0 = term ? 0 : lc[0], c1 = term ? 0 : lc[1], c2 = term ? 0 : lc[2];
+        const bool testing = active && !hit_any;
+        const int c0 = testing ? lc[0] : 0, c1 = testing ? lc[1] : 0, c2 = testing ? lc[2] : 0;
         const int total = parked == 0 ? 0 : c0 + (parked > 1 ? c1 : 0) + (parked > 2 ? c2 : 0);
         const int kmax = __reduce_max_sync(FULL, total);
         for (int k = 0; k < kmax; ++k) {
-            if (k >= total || term) continue;
+            if (k >= total || hit_any) continue;
             const int slot = k < c0 ? ls[0] + k : (k < c0 + c1 ? ls[1] + (k - c0) : ls[2] + (k - c0 - c1));
             const float4 A = __ldg(S.tris + 3 * (size_t)slot), B = __ldg(S.tris + 3 * (size_t)slot + 1),
                          C = __ldg(S.tris + 3 * (size_t)slot + 2);
             float t, u, v;
             if (!mt_test(o, r.d, A, B, C, &t, &u, &v)) continue;
             if (!(t > r.tmin && t < r.tmax)) continue;
-            if (ANY) { found = true; term = true; continue; }
+            if (ANY) { found = true; hit_any = true; continue; }
             const uint32_t key = __float_as_uint(A.w);
             bool better = t < best_t;
             if (!better && t == best_t && found)
@@ -267,17 +324,20 @@ __device__ __forceinline__ bool trace_warp(const DevScene& S, const TraceRay& r,
             if (better) {
                 best_t = t;
                 found = true;
-                hit->t = t; hit->u = u; hit->v = v;
-                hit->inst = inst; hit->tri = slot;
+                hit.t = t; hit.u = u; hit.v = v;
+                hit.inst = inst; hit.tri = slot;
                 best_key = key;
                 best_orig = inst_orig;
             }
         }
         parked = 0;
         lc[0] = lc[1] = lc[2] = 0;
-        if (exhausted) term = true;
+        // ---- finished rays hand over their result; the lane becomes idle
+        if (active && (exhausted || hit_any)) {
+            src.store(id, r, hit, found);
+            active = false;
+        }
     }
-    return found;
 }
 
 // DiffuseAreaQuadLight::intersect_plane (light.rs:86-107).
@@ -298,16 +358,10 @@ __device__ __forceinline__ bool quad_intersect(const DevQuadLight& L, const f3& 
     return true;
 }
 
-// Closest hit including quad lights (lights after primitives with strict `<`,
-// scene.rs:78-94).
-// All lanes of the warp must call it (see trace_warp).
-// `root` is the top-level BVH to trace (S.tlas_root, or a batch part's) and
-// [light_first, light_first + light_count) the quad lights it can hit.
-__device__ __forceinline__ void trace_closest_with_lights(const DevScene& S, const TraceRay& r, bool valid,
-                                                          int32_t root, uint32_t light_first, uint32_t light_count,
-                                                          TraceHit* hit) {
-    trace_warp<false>(S, r, valid, root, hit);
-    if (!valid) return;
+// Quad lights after primitives with strict `<` (scene.rs:78-94): lights
+// [light_first, light_first + light_count) can replace the closest hit.
+__device__ __forceinline__ void hit_quad_lights(const DevScene& S, const TraceRay& r, uint32_t light_first,
+                                                uint32_t light_count, TraceHit* hit) {
     float best = hit->inst >= 0 ? hit->t : r.tmax;
     for (uint32_t l = light_first; l < light_first + light_count; ++l) {
         float t; f3 p;

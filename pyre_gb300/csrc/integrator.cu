@@ -32,6 +32,7 @@ namespace cg = cooperative_groups;
 namespace pyre {
 
 #define PYRE_MAX_DEPTH 64
+#define PYRE_SORT_BINS 1024  // shade-queue sort keys: escaped, light hit, then materials
 
 struct WaveCtl {
     uint32_t wave;
@@ -42,6 +43,9 @@ struct WaveCtl {
     uint32_t scount[PYRE_MAX_DEPTH];      // shadow queue sizes per depth
     uint32_t fetch[2 * PYRE_MAX_DEPTH];   // work counters of extend / shadow
     unsigned long long extend_rays, shadow_rays, samples;
+    // material sort of the shade queue: bin sizes (zero between sorts) and bin offsets
+    uint32_t sort_hist[PYRE_SORT_BINS];
+    uint32_t sort_off[PYRE_SORT_BINS];
 };
 
 // Batched rendering: per-job view, per-wave segments (a segment = one job's
@@ -84,7 +88,15 @@ struct WaveParams {
     float* env_grad;     // env texels*3 or null
     uint32_t n_mat;
     int smem_grad;       // material gradients summed per block in shared memory
+    int refill;          // traversal: idle lanes of a warp that trigger a refetch
+    int sort;            // shade reads the live paths sorted by material (P.qsort)
 };
+
+#define PYRE_DEFAULT_REFILL 16
+static inline int refill_lanes(const pyre_render_params* rp) {
+    const uint32_t v = rp ? rp->refill_lanes : 0u;
+    return v == 0 ? PYRE_DEFAULT_REFILL : (int)std::min<uint32_t>(v, 32u);
+}
 
 #define PYRE_GSLOT 4  // float4s of parked gradient terms per NEE slot
 
@@ -102,6 +114,7 @@ struct PathSoA {
     float4* sh_o;      // ns per path: shadow origin.xyz, t_max
     float4* sh_d;      // ns per path: shadow direction.xyz, time
     uint32_t* q[2];
+    uint32_t* qsort;   // the live paths of the current depth ordered by shade_key
     uint32_t* sq;
     float4* acc_r;     // per crop pixel: radiance sum.xyz, depth sum
     float4* acc_a;     // albedo sum
@@ -228,81 +241,72 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
 }
 
 // ---------------------------------------------------------------- extend --
+// Closest hit of the live paths (Scene::intersect, scene.rs:57-97).
 template <bool BATCH>
-__global__ void __launch_bounds__(128) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
-    const uint32_t n = P.ctl->count[depth];
-    const uint32_t* qin = P.q[depth & 1];
-    uint32_t* fetch = &P.ctl->fetch[2 * depth];
-    const int lane = threadIdx.x & 31;
-    while (true) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(fetch, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const uint32_t j = base + lane;
-        const bool valid = j < n;
-        const uint32_t i = !valid ? 0u : (depth == 0 ? j : qin[j]);
-        TraceRay r;
+struct ExtendRays {
+    const DevScene* S;
+    const PathSoA* P;
+    const WaveParams* W;
+    const uint32_t* qin;  // live-path queue; null at depth 0 (path j)
+    __device__ __forceinline__ uint32_t load(uint32_t j, TraceRay& r, int32_t& root) const {
+        const uint32_t i = qin ? qin[j] : j;
+        const float4 ro = P->ray_o[i], rd = P->ray_d[i];
+        r.o = mk3(ro.x, ro.y, ro.z);
+        r.d = mk3(rd.x, rd.y, rd.z);
         r.tmin = 1e-4f;
         r.tmax = __int_as_float(0x7f800000);
-        if (valid) {
-            const float4 ro = P.ray_o[i], rd = P.ray_d[i];
-            r.o = mk3(ro.x, ro.y, ro.z);
-            r.d = mk3(rd.x, rd.y, rd.z);
-            r.time = rd.w;
-        } else {
-            r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.time = 0.0f;
-        }
-        int32_t root = S.tlas_root;
-        uint32_t lfirst = 0, lcount = S.n_lights;
-        if (BATCH && valid) {
-            const DevJob& J = W.jobs[P.pjob[i]];
-            root = J.tlas_root; lfirst = J.light_first; lcount = J.light_count;
-        }
-        TraceHit h;
-        trace_closest_with_lights(S, r, valid, root, lfirst, lcount, &h);
-        if (valid) {
-            const int32_t code = h.light >= 0 ? -2 - h.light : h.inst;
-            P.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
-            P.hit_inst[i] = code;
-        }
+        r.time = rd.w;
+        root = BATCH ? W->jobs[P->pjob[i]].tlas_root : S->tlas_root;
+        return i;
     }
+    __device__ __forceinline__ void store(uint32_t i, const TraceRay& r, TraceHit& h, bool) const {
+        uint32_t lfirst = 0, lcount = S->n_lights;
+        if (BATCH) {
+            const DevJob& J = W->jobs[P->pjob[i]];
+            lfirst = J.light_first; lcount = J.light_count;
+        }
+        hit_quad_lights(*S, r, lfirst, lcount, &h);
+        P->hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+        P->hit_inst[i] = h.light >= 0 ? -2 - h.light : h.inst;
+    }
+};
+
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+    ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1]};
+    trace_stream<false>(S, src, P.ctl->count[depth], &P.ctl->fetch[2 * depth], W.refill);
 }
 
 // ---------------------------------------------------------------- shadow --
+// Visibility of the parked NEE contributions (Scene::occluded /
+// occluded_dir, scene.rs:102-140): an occluded ray clears its slot.
+template <bool BATCH>
+struct ShadowRays {
+    const DevScene* S;
+    const PathSoA* P;
+    const WaveParams* W;
+    __device__ __forceinline__ uint32_t load(uint32_t j, TraceRay& r, int32_t& root) const {
+        const uint32_t target = P->sq[j];
+        const float4 so = P->sh_o[target], sd = P->sh_d[target];
+        r.o = mk3(so.x, so.y, so.z);
+        r.d = mk3(sd.x, sd.y, sd.z);
+        r.tmin = 1e-3f;
+        r.tmax = so.w;
+        r.time = sd.w;
+        root = BATCH ? W->jobs[P->pjob[target / W->ns]].tlas_root : S->tlas_root;
+        return target;
+    }
+    __device__ __forceinline__ void store(uint32_t target, const TraceRay&, TraceHit&, bool occluded) const {
+        if (!occluded) return;
+        P->pend[target] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (P->gpend) P->gpend[PYRE_GSLOT * (size_t)target + 1].w = 0.0f;  // its gradient terms die with it
+    }
+};
+
 template <bool BATCH>
 __global__ void __launch_bounds__(128) k_shadow(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
-    const uint32_t n = P.ctl->scount[depth];
-    uint32_t* fetch = &P.ctl->fetch[2 * depth + 1];
-    const int lane = threadIdx.x & 31;
-    while (true) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(fetch, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const uint32_t j = base + lane;
-        const bool valid = j < n;
-        const uint32_t target = valid ? P.sq[j] : 0u;
-        TraceRay r;
-        r.tmin = 1e-3f;
-        if (valid) {
-            const float4 so = P.sh_o[target], sd = P.sh_d[target];
-            r.o = mk3(so.x, so.y, so.z);
-            r.d = mk3(sd.x, sd.y, sd.z);
-            r.tmax = so.w;
-            r.time = sd.w;
-        } else {
-            r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.tmax = 0.0f; r.time = 0.0f;
-        }
-        int32_t root = S.tlas_root;
-        if (BATCH && valid) root = W.jobs[P.pjob[target / W.ns]].tlas_root;
-        TraceHit h;
-        const bool occluded = trace_warp<true>(S, r, valid, root, &h);
-        if (valid && occluded) {
-            P.pend[target] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (P.gpend) P.gpend[PYRE_GSLOT * (size_t)target + 1].w = 0.0f;  // its gradient terms die with it
-        }
-    }
+    ShadowRays<BATCH> src{&S, &P, &W};
+    trace_stream<true>(S, src, P.ctl->scount[depth], &P.ctl->fetch[2 * depth + 1], W.refill);
 }
 
 // ------------------------------------------------------- adjoint helpers --
@@ -340,6 +344,75 @@ __device__ __forceinline__ void apply_parked_grad(const DevScene& S, const WaveP
     }
 }
 
+// ------------------------------------------------------- material sort --
+// Counting sort of the live paths by what shade will run for them: escaped
+// paths, quad-light hits, then one bin per material (modulo the bin count).
+// Shade then sees warps of one material, with one code path (Lambertian or
+// Disney) and the same material record. Results do not depend on the order
+// in which shade visits paths.
+__device__ __forceinline__ uint32_t shade_key(const DevScene& S, int32_t code) {
+    if (code == -1) return 0u;
+    if (code <= -2) return 1u;
+    return 2u + S.inst[code].material % (uint32_t)(PYRE_SORT_BINS - 2);
+}
+
+__global__ void k_sort_count(DevScene S, PathSoA P, uint32_t depth) {
+    const uint32_t n = P.ctl->count[depth];
+    const uint32_t* qin = P.q[depth & 1];
+    const int lane = threadIdx.x & 31;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t i = depth == 0 ? j : qin[j];
+        const uint32_t key = shade_key(S, P.hit_inst[i]);
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        if (lane == __ffs(peers) - 1) atomicAdd(&P.ctl->sort_hist[key], (uint32_t)__popc(peers));
+    }
+}
+
+// One block of PYRE_SORT_BINS threads: exclusive scan of the bin sizes into
+// the bin offsets; the sizes are cleared for the next sort.
+__global__ void __launch_bounds__(PYRE_SORT_BINS) k_sort_scan(PathSoA P) {
+    __shared__ uint32_t warp_sum[PYRE_SORT_BINS / 32];
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t v = P.ctl->sort_hist[t];
+    P.ctl->sort_hist[t] = 0;
+    uint32_t x = v;  // inclusive scan within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) warp_sum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (uint32_t)o) w += y;
+        }
+        warp_sum[lane] = w;  // inclusive sums of the warps
+    }
+    __syncthreads();
+    P.ctl->sort_off[t] = (warp ? warp_sum[warp - 1] : 0u) + x - v;
+}
+
+__global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
+    const uint32_t n = P.ctl->count[depth];
+    const uint32_t* qin = P.q[depth & 1];
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t i = depth == 0 ? j : qin[j];
+        const uint32_t key = shade_key(S, P.hit_inst[i]);
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&P.ctl->sort_off[key], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        P.qsort[base + __popc(peers & below)] = i;
+    }
+}
+
 // ----------------------------------------------------------------- shade --
 // One path vertex of PathIntegrator::integrate (integrator.rs:242-388).
 // ADJ: the path-replay adjoint of the same vertex (pyre_backward): the same
@@ -359,7 +432,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams
     const bool last_was_specular = depth == 0;  // no specular BSDFs: only camera rays
     const float INF = __int_as_float(0x7f800000);
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t i = depth == 0 ? j : qin[j];
+        const uint32_t i = W.sort ? P.qsort[j] : (depth == 0 ? j : qin[j]);
         float4 Lq = P.L[i];
         f3 L = mk3(Lq.x, Lq.y, Lq.z);
         f3 delta = splat3(0.0f), Ltot = splat3(0.0f);
@@ -696,51 +769,45 @@ __global__ void k_finalize(PathSoA P, uint32_t npix, float inv_spp, float* rad, 
 }
 
 // ------------------------------------------------------ ray-query kernels --
-template <bool ANY>
-__global__ void __launch_bounds__(128) k_intersect(DevScene S, const float* __restrict__ org, const float* __restrict__ dir,
-                                                   const float* __restrict__ tmin, const float* __restrict__ tmax,
-                                                   const float* __restrict__ time, uint32_t n, unsigned int* counter,
-                                                   int32_t* kind, int32_t* inst, int32_t* tri, float* tt, float* uu,
-                                                   float* vv, uint8_t* occluded) {
-    const int lane = threadIdx.x & 31;
-    while (true) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(counter, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + lane;
-        const bool valid = i < n;
-        TraceRay r;
-        if (valid) {
-            r.o = mk3(org[3 * (size_t)i], org[3 * (size_t)i + 1], org[3 * (size_t)i + 2]);
-            r.d = mk3(dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]);
-            r.tmin = tmin[i];
-            r.tmax = tmax[i];
-            r.time = time ? time[i] : 0.0f;
+// Rays and results of pyre_intersect_closest / pyre_intersect_any (caller
+// arrays, SoA).
+struct QueryRays {
+    const DevScene* S;
+    const float* org; const float* dir; const float* tmin; const float* tmax; const float* time;
+    int32_t* kind; int32_t* inst; int32_t* tri; float* tt; float* uu; float* vv; uint8_t* occluded;
+    __device__ __forceinline__ uint32_t load(uint32_t i, TraceRay& r, int32_t& root) const {
+        r.o = mk3(org[3 * (size_t)i], org[3 * (size_t)i + 1], org[3 * (size_t)i + 2]);
+        r.d = mk3(dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]);
+        r.tmin = tmin[i];
+        r.tmax = tmax[i];
+        r.time = time ? time[i] : 0.0f;
+        root = S->tlas_root;
+        return i;
+    }
+    __device__ __forceinline__ void store(uint32_t i, const TraceRay& r, TraceHit& h, bool found) const {
+        if (occluded) { occluded[i] = found ? 1 : 0; return; }
+        hit_quad_lights(*S, r, 0, S->n_lights, &h);
+        if (h.light >= 0) {
+            kind[i] = 2; inst[i] = h.light; tri[i] = -1;
+            tt[i] = h.t; uu[i] = 0.0f; vv[i] = 0.0f;
+        } else if (h.inst >= 0) {
+            kind[i] = 1;
+            inst[i] = S->inst[h.inst].orig_id;
+            tri[i] = (int32_t)__float_as_uint(__ldg(S->tris + 3 * (size_t)h.tri).w);
+            tt[i] = h.t; uu[i] = h.u; vv[i] = h.v;
         } else {
-            r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.tmin = 0.0f; r.tmax = 0.0f; r.time = 0.0f;
-        }
-        TraceHit h;
-        if (ANY) {
-            const bool occ = trace_warp<true>(S, r, valid, S.tlas_root, &h);
-            if (valid) occluded[i] = occ ? 1 : 0;
-        } else {
-            trace_closest_with_lights(S, r, valid, S.tlas_root, 0, S.n_lights, &h);
-            if (!valid) continue;
-            if (h.light >= 0) {
-                kind[i] = 2; inst[i] = h.light; tri[i] = -1;
-                tt[i] = h.t; uu[i] = 0.0f; vv[i] = 0.0f;
-            } else if (h.inst >= 0) {
-                kind[i] = 1;
-                inst[i] = S.inst[h.inst].orig_id;
-                tri[i] = (int32_t)__float_as_uint(__ldg(S.tris + 3 * (size_t)h.tri).w);
-                tt[i] = h.t; uu[i] = h.u; vv[i] = h.v;
-            } else {
-                kind[i] = 0; inst[i] = -1; tri[i] = -1;
-                tt[i] = __int_as_float(0x7f800000); uu[i] = 0.0f; vv[i] = 0.0f;
-            }
+            kind[i] = 0; inst[i] = -1; tri[i] = -1;
+            tt[i] = __int_as_float(0x7f800000); uu[i] = 0.0f; vv[i] = 0.0f;
         }
     }
+};
+
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_intersect(DevScene S, QueryRays q, uint32_t n, unsigned int* counter,
+                                                   int refill) {
+    QueryRays src = q;
+    src.S = &S;
+    trace_stream<ANY>(S, src, n, counter, refill);
 }
 
 // ------------------------------------------------------------ host side --
@@ -784,6 +851,7 @@ size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* ou
     s.sh_d = c.take<float4>(P * ns);
     s.q[0] = c.take<uint32_t>(P);
     s.q[1] = c.take<uint32_t>(P);
+    s.qsort = c.take<uint32_t>(P);
     s.sq = c.take<uint32_t>(P * ns);
     s.acc_r = c.take<float4>(npix);
     s.acc_a = c.take<float4>(npix);
@@ -800,7 +868,7 @@ size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* ou
 struct Launch {
     int block_shade = 256;  // raygen, shade, accumulate (at most 256)
     int block_trace = 128;  // extend, shadow (at most 128)
-    int grid_raygen, grid_shade, grid_extend, grid_shadow, grid_acc;
+    int grid_raygen, grid_shade, grid_extend, grid_shadow, grid_acc, grid_sort;
 };
 
 // Grid sizes for the stage kernels: persistent grids of resident blocks.
@@ -819,6 +887,7 @@ Launch make_launch(pyre_ctx* ctx, uint32_t block_size) {
     L.grid_extend = grid_for(ctx, k_extend<BATCH>, L.block_trace);
     L.grid_shadow = grid_for(ctx, k_shadow<BATCH>, L.block_trace);
     L.grid_acc = BATCH ? grid_for(ctx, k_accumulate_batch, L.block_shade) : grid_for(ctx, k_accumulate, L.block_shade);
+    L.grid_sort = grid_for(ctx, k_sort_scatter, 256);
     return L;
 }
 
@@ -838,6 +907,14 @@ void mark(pyre_ctx* ctx, int tag) {
 
 enum { STAGE_EXTEND = 0, STAGE_SHADE = 1, STAGE_SHADOW = 2, STAGE_OTHER = 3, STAGE_END = 4 };
 
+// Orders the live paths of depth d by shade_key into P.qsort.
+void enqueue_sort(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Launch& Lc, uint32_t d) {
+    cudaStream_t st = ctx->stream;
+    k_sort_count<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
+    k_sort_scan<<<1, PYRE_SORT_BINS, 0, st>>>(P);
+    k_sort_scatter<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
+}
+
 void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const WaveParams& W, const Launch& Lc) {
     cudaStream_t st = ctx->stream;
     mark(ctx, STAGE_OTHER);
@@ -847,6 +924,7 @@ void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Wave
         mark(ctx, STAGE_EXTEND);
         k_extend<false><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
         mark(ctx, STAGE_SHADE);
+        if (W.sort) enqueue_sort(ctx, S, P, Lc, d);
         k_shade<false><<<Lc.grid_shade, Lc.block_shade, 0, st>>>(S, P, W, d);
         if (W.ns > 0) {
             mark(ctx, STAGE_SHADOW);
@@ -870,6 +948,7 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
         mark(ctx, STAGE_EXTEND);
         k_extend<true><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
         mark(ctx, STAGE_SHADE);
+        if (W.sort) enqueue_sort(ctx, S, P, Lc, d);
         k_shade<true><<<Lc.grid_shade, Lc.block_shade, 0, st>>>(S, P, W, d);
         if (W.ns > 0) {
             mark(ctx, STAGE_SHADOW);
@@ -882,7 +961,9 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
     mark(ctx, STAGE_END);
 }
 
-uint32_t kernels_per_wave(const WaveParams& W) { return 4 + W.max_depth * (W.ns > 0 ? 3 : 2); }
+uint32_t kernels_per_wave(const WaveParams& W) {
+    return 4 + W.max_depth * ((W.ns > 0 ? 3 : 2) + (W.sort ? 3 : 0));
+}
 
 }  // namespace
 }  // namespace pyre
@@ -930,6 +1011,8 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     W.max_depth = rp.max_depth; W.min_rr = rp.min_rr_depth;
     W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
+    W.refill = refill_lanes(&rp);
+    W.sort = rp.sort_by_material ? 1 : 0;
     const uint32_t spp = rp.spp_end - rp.spp_begin;
     uint64_t target = rp.wave_paths ? rp.wave_paths : (uint64_t)8 << 20;
     uint64_t K = std::max<uint64_t>(1, target / W.npix);
@@ -962,9 +1045,9 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     if (rp.use_graph && !ctx->stage_timing && !keep) {
         // One wave captured once per configuration, replayed `waves` times.
         char key[256];
-        std::snprintf(key, sizeof key, "%llu/%p/%u/%u/%u/%u/%u/%u/%u/%u/%d", (unsigned long long)scene->serial, ctx->render_ws.ptr,
-                      W.npix, W.k_per_wave, W.max_depth, W.min_rr, W.ns, W.spp_begin, W.spp_end, W.cx0 + W.cy0 * 65536u,
-                      W.env_cdf);
+        std::snprintf(key, sizeof key, "%llu/%p/%u/%u/%u/%u/%u/%u/%u/%u/%d/r%d/s%d", (unsigned long long)scene->serial,
+                      ctx->render_ws.ptr, W.npix, W.k_per_wave, W.max_depth, W.min_rr, W.ns, W.spp_begin, W.spp_end,
+                      W.cx0 + W.cy0 * 65536u, W.env_cdf, W.refill, W.sort);
         std::string k2 = std::string(key) + "/" + std::to_string(W.width) + "x" + std::to_string(W.height) + "/b" +
                          std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace);
         // camera bytes are part of the key
@@ -1105,6 +1188,8 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     std::memset(&W, 0, sizeof W);
     W.max_depth = max_depth;
     W.ns = scene->part_light_max;
+    W.refill = refill_lanes(params);
+    W.sort = params && params->sort_by_material ? 1 : 0;
     const uint32_t ns = std::max(W.ns, 1u);
 
     // ---- workspace: path state, accumulators, tables, staging film
@@ -1144,7 +1229,8 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
         std::string key = "batch/" + std::to_string(scene->serial) + "/" +
                           std::to_string((uintptr_t)ctx->render_ws.ptr) + "/" + std::to_string(n_waves) + "/" +
                           std::to_string(max_depth) + "/" + std::to_string(max_paths) + "/b" +
-                          std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace) + "/";
+                          std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace) + "/r" +
+                          std::to_string(W.refill) + "/s" + std::to_string(W.sort) + "/";
         key.append(reinterpret_cast<const char*>(dj.data()), job_bytes);
         if (!ctx->wave_graph || ctx->wave_graph_key != key) {
             if (ctx->wave_graph) { cudaGraphExecDestroy(ctx->wave_graph); ctx->wave_graph = nullptr; }
@@ -1246,6 +1332,8 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     W.max_depth = rp.max_depth; W.min_rr = rp.min_rr_depth;
     W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
+    W.refill = refill_lanes(&rp);
+    W.sort = rp.sort_by_material ? 1 : 0;
     const uint32_t ns = std::max(W.ns, 1u);
     const size_t cap = PYRE_NOALLOC_SCRATCH_BYTES;
     if (carve_paths(nullptr, W.npix, ns, W.npix, nullptr) > cap) {
@@ -1356,14 +1444,16 @@ static int intersect_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_ray
         }
     }
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), st));
+    QueryRays q{};
+    q.org = org; q.dir = dir; q.tmin = tmin; q.tmax = tmax; q.time = time;
     if (any) {
+        q.occluded = occ;
         int grid = grid_for(ctx, k_intersect<true>, 128);
-        k_intersect<true><<<grid, 128, 0, st>>>(scene->dev, org, dir, tmin, tmax, time, (uint32_t)n, ctx->d_counter,
-                                                nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, occ);
+        k_intersect<true><<<grid, 128, 0, st>>>(scene->dev, q, (uint32_t)n, ctx->d_counter, PYRE_DEFAULT_REFILL);
     } else {
+        q.kind = kind; q.inst = inst; q.tri = tri; q.tt = tt; q.uu = uu; q.vv = vv;
         int grid = grid_for(ctx, k_intersect<false>, 128);
-        k_intersect<false><<<grid, 128, 0, st>>>(scene->dev, org, dir, tmin, tmax, time, (uint32_t)n, ctx->d_counter,
-                                                 kind, inst, tri, tt, uu, vv, nullptr);
+        k_intersect<false><<<grid, 128, 0, st>>>(scene->dev, q, (uint32_t)n, ctx->d_counter, PYRE_DEFAULT_REFILL);
     }
     PYRE_CUDA_TRY(ctx, cudaGetLastError());
     if (mem == PYRE_MEM_HOST) {
@@ -1477,6 +1567,8 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     W.max_depth = rp.max_depth; W.min_rr = rp.min_rr_depth;
     W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
+    W.refill = refill_lanes(&rp);
+    W.sort = rp.sort_by_material ? 1 : 0;
     const uint32_t spp = rp.spp_end - rp.spp_begin;
     uint64_t K = std::max<uint64_t>(1, (rp.wave_paths ? rp.wave_paths : (uint64_t)8 << 20) / W.npix);
     K = std::min<uint64_t>(K, spp);
@@ -1527,6 +1619,7 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
         k_raygen<false><<<Lc.grid_raygen, Lc.block_shade, 0, st>>>(S, W);
         for (uint32_t d = 0; d < W.max_depth; ++d) {
             k_extend<false><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(D, S, W, d);
+            if (W.sort) enqueue_sort(ctx, D, S, Lc, d);
             k_shade<false, true><<<grid_adj, Lc.block_shade, smem, st>>>(D, S, W, d);
             if (W.ns > 0) k_shadow<false><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(D, S, W, d);
         }

@@ -96,7 +96,8 @@ class RenderParams(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("spp_begin", C.c_uint32), ("spp_end", C.c_uint32),
                 ("max_depth", C.c_uint32), ("min_rr_depth", C.c_uint32), ("crop", C.c_uint32 * 4),
                 ("env_sampling", C.c_uint32), ("wave_paths", C.c_uint32), ("block_size", C.c_uint32),
-                ("sort_by_material", C.c_uint32), ("use_graph", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+                ("sort_by_material", C.c_uint32), ("use_graph", C.c_uint32), ("refill_lanes", C.c_uint32),
+                ("reserved", C.c_uint32 * 3)]
 
 
 class Film(C.Structure):

@@ -89,3 +89,24 @@ def test_procedural_studio_small(gpu_ctx, oracle_mod):
     film = gpu_ctx.render(ds, cam, PathIntegrator(8, 3), 160, 90, 8, env_sampling=PYRE_ENV_CDF)
     ref = oracle_mod.OracleScene(sc).render(cam, 160, 90, 8)
     _check(film, ref, bar=1e-2)
+
+
+@pytest.mark.parametrize("refill,sort", [(1, 0), (4, 0), (32, 0), (8, 1), (32, 1)])
+def test_traversal_and_shade_order_do_not_change_results(gpu_ctx, refill, sort):
+    """The traversal kernels refetch rays into finished lanes, and shade can
+    visit the live paths sorted by material; neither the lane, the warp nor
+    the order in which a path is processed may change any bit of the film."""
+    from pyre_gb300 import native as N
+    from pyre_gb300.scene import Film
+    sc = P.studio_procedural(n_side=3, segments=24, n_moving=2, hdri_size=(256, 128))
+    cam = P.studio_procedural_camera(96, 64)
+    ds = gpu_ctx.upload(sc)
+    it = PathIntegrator(8, 3)
+    base = gpu_ctx.render(ds, cam, it, 96, 64, 4)
+    film = Film(96, 64)
+    p = gpu_ctx.params(96, 64, 0, 4, it, refill_lanes=refill)
+    p.sort_by_material = sort
+    f = N.Film(N.fptr(film.radiance), N.fptr(film.albedo), N.fptr(film.normal), N.fptr(film.depth), N.PYRE_MEM_HOST)
+    gpu_ctx.render_into(ds, cam, p, f)
+    for ch in ("radiance", "albedo", "normal", "depth"):
+        np.testing.assert_array_equal(getattr(film, ch), getattr(base, ch))
