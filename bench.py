@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=0, help="rows in the CPU sample (0 = auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--graph", type=int, default=0, help="replay waves through a CUDA graph")
+    ap.add_argument("--bvh-width", type=int, default=0, help="instance BVH width 2, 4 or 8 (0 = 2)")
     ap.add_argument("--refill", type=int, default=0,
                     help="traversal: idle lanes of a warp that trigger a ray refetch (0 = library default)")
     ap.add_argument("--workload", default="studio", choices=["studio", "batch", "adjoint"],
@@ -150,7 +151,8 @@ def run_batch(args):
     samples = sum(j["width"] * j["height"] * j["spp"] for j in jobs)
     best, trials = autotune.tune_batch(ctx, ds, spec)
     knobs = dict(wave_paths=best["wave_paths"], use_graph=best["use_graph"], block_size=best["block_size"],
-                 sort_by_material=best.get("sort_by_material", 0), refill_lanes=best.get("refill_lanes", 0))
+                 sort_by_material=best.get("sort_by_material", 0), refill_lanes=best.get("refill_lanes", 0),
+                 bvh_width=best.get("bvh_width", 0))
     for _ in range(args.warmup):
         ctx.render_batch(ds, spec, **knobs)
     batch_ms = []
@@ -328,7 +330,7 @@ def main():
     # Weak scaling: rank r renders samples [r*64, (r+1)*64) of the frame.
     s0 = rank * SPP
     params = CudaIntegrator.params(W, H, s0, s0 + SPP, integ, env_sampling=N.PYRE_ENV_ALIAS, use_graph=args.graph,
-                                    refill_lanes=args.refill)
+                                    refill_lanes=args.refill, bvh_width=args.bvh_width)
     npix = W * H
     dev = {k: torch.empty(npix * c, dtype=torch.float32, device="cuda") for k, c in
            (("radiance", 3), ("albedo", 3), ("normal", 3), ("depth", 1))}
@@ -419,7 +421,7 @@ def main():
                        "l2": "inputs larger than L2 (scene %.0f MB + path state)" % (info.device_bytes / 1e6),
                        "triangles": int(info.n_triangles), "scene_gen_s": round(gen_s, 2),
                        "scene_upload_s": round(upload_s, 2), "use_graph": args.graph,
-                       "refill_lanes": args.refill},
+                       "refill_lanes": args.refill, "bvh_width": args.bvh_width},
             "mrays_per_s": (ext_rays + shadow_rays) * world / t_max / 1e6,
             "rays": {"extend": ext_rays // args.steps, "shadow": shadow_rays // args.steps},
             "wall_s_timed": wall,

@@ -160,6 +160,12 @@ typedef struct pyre_scene_info {
 } pyre_scene_info;
 int pyre_scene_get_info(const pyre_scene* scene, pyre_scene_info* out);
 
+/* Default instance-BVH width of the scene's traversals (2, 4 or 8; no
+ * reference counterpart: Bvh is binary, bvh.rs:18-30). Width 4 and 8 BVHs are
+ * collapsed from the binary one (same boxes, leaves and triangles, so the
+ * same hits) the first time they are needed and kept with the scene. */
+int pyre_scene_set_bvh_width(pyre_ctx* ctx, pyre_scene* scene, uint32_t width);
+
 /* --------------------------------------------------------- Intersect --- */
 
 /* Rays as the caller built them (directions are NOT normalized), like the
@@ -225,7 +231,9 @@ typedef struct pyre_render_params {
     uint32_t use_graph;              /* capture one wave as a CUDA graph and replay it */
     uint32_t refill_lanes;           /* traversal: refetch rays once this many lanes of a
                                         warp are idle (1-32); 0 = 16 */
-    uint32_t reserved[3];
+    uint32_t bvh_width;              /* instance BVH width 2, 4 or 8; 0 = the scene's
+                                        (pyre_scene_set_bvh_width) */
+    uint32_t reserved[2];
 } pyre_render_params;
 
 /* Film: per-pixel means over the sample range (PixelSample fields,
@@ -255,6 +263,18 @@ typedef struct pyre_render_stats {
  * once per (pixel, sample) with IndependentSampler(pixel_seed(x, y, s)). */
 int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
                 const pyre_render_params* params, pyre_film* film);
+
+/* Progressive accumulation (the viewer's headless render loop,
+ * crates/pyre/src/viewer.rs:114-185): renders passes s in
+ * [spp_begin, spp_end), one sample per pixel each with sample index s, and
+ * merges each into the running radiance mean in pass order,
+ * mean += (L_s - mean) / (s + 1), in binary32 like the viewer. `mean_rgb`
+ * (crop width x height x 3 floats, host or device per `mem`) holds the mean of
+ * passes [0, spp_begin) on entry (ignored when spp_begin is 0) and of
+ * [0, spp_end) on return. Calls may be chained: passes [0, a) then [a, b)
+ * give the same bits as [0, b). */
+int pyre_render_progressive(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                            const pyre_render_params* params, float* mean_rgb, int mem);
 int pyre_get_render_stats(const pyre_ctx* ctx, pyre_render_stats* out);
 
 /* ----------------------------------------------------------- Adjoint --- */

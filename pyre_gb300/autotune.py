@@ -4,9 +4,8 @@ Knobs (pyre_render_params): wave_paths (queue capacity = paths in flight per
 wave), block_size (threads per block of the shade-type kernels; the trace
 kernels use min(block_size, 128)), use_graph (CUDA-graph replay),
 sort_by_material (shade visits the live paths sorted by material) and
-refill_lanes (a warp refetches rays once this many of its lanes are idle).
-BVH width is fixed at 2 (the device node layout is binary) and reported as a
-single-valued knob.
+refill_lanes (a warp refetches rays once this many of its lanes are idle) and
+bvh_width (instance BVHs traversed as binary, 4-wide or 8-wide nodes).
 
 Search: coordinate descent from the defaults (each knob swept with the others
 fixed, best kept), timed with the library's CUDA events. Results are cached in
@@ -24,7 +23,7 @@ KNOBS = {
     "wave_paths": [2 << 20, 4 << 20, 8 << 20, 16 << 20],
     "block_size": [128, 256],
     "use_graph": [0, 1],
-    "bvh_width": [2],
+    "bvh_width": [2, 4, 8],
     "sort_by_material": [0, 1],
     "refill_lanes": [4, 8, 16, 32],
 }
@@ -100,7 +99,7 @@ def tune_batch(ctx, dscene, spec: list, reps: int = 1, use_cache: bool = True):
     def run(knobs):
         ctx.render_batch(dscene, spec, wave_paths=knobs["wave_paths"], use_graph=knobs["use_graph"],
                          block_size=knobs["block_size"], sort_by_material=knobs["sort_by_material"],
-                         refill_lanes=knobs["refill_lanes"])
+                         refill_lanes=knobs["refill_lanes"], bvh_width=knobs["bvh_width"])
         return ctx.stats().ms_total
 
     return tune(run, key, reps, use_cache)
@@ -118,7 +117,8 @@ def tune_render(ctx, dscene, camera, integrator, width: int, height: int, spp: i
     def run(knobs):
         p = CudaIntegrator.params(width, height, 0, spp, integrator, env_sampling=env_sampling,
                                   wave_paths=knobs["wave_paths"], use_graph=knobs["use_graph"],
-                                  block_size=knobs["block_size"], refill_lanes=knobs["refill_lanes"])
+                                  block_size=knobs["block_size"], refill_lanes=knobs["refill_lanes"],
+                                  bvh_width=knobs["bvh_width"])
         p.sort_by_material = knobs["sort_by_material"]
         ctx.render_into(dscene, camera, p, N.Film(N.fptr(out), None, None, None, N.PYRE_MEM_HOST))
         return ctx.stats().ms_total

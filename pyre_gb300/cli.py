@@ -36,6 +36,7 @@ def parse(argv=None):
     ap.add_argument("--rays", type=int, default=1 << 24, help="microbench: number of rays")
     ap.add_argument("--query", default="closest", choices=["closest", "any", "both"])
     ap.add_argument("--level", type=int, default=8, help="microbench: icosphere subdivision level")
+    ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 4, 8], help="instance BVH width")
     return ap.parse_args(argv)
 
 
@@ -62,6 +63,7 @@ def microbench(args, ctx) -> int:
     mesh = sc.primitives[0].instance.mesh
     org, d, tmin, tmax = P.random_rays(mesh, args.rays, seed=1)
     ds = ctx.upload(sc)
+    ds.set_bvh_width(args.bvh_width)
     dev = {k: torch.from_numpy(v).cuda() for k, v in (("o", org), ("d", d), ("tmin", tmin), ("tmax", tmax))}
     rays = N.Rays(N.dptr(dev["o"]), N.dptr(dev["d"]), N.dptr(dev["tmin"]), N.dptr(dev["tmax"]), None)
     n = args.rays
@@ -82,8 +84,8 @@ def microbench(args, ctx) -> int:
                 ctx.check(ctx.lib.pyre_intersect_any(ctx.handle, ds.handle, C.byref(rays), n,
                                                      N.dptr(occ, C.c_uint8), N.PYRE_MEM_DEVICE))
             dt = time.perf_counter() - t0
-            print(json.dumps({"query": q, "rays": n, "triangles": mesh.triangle_count(), "elapsed_ms": dt * 1e3,
-                              "mrays_per_s": n / dt / 1e6}), flush=True)
+            print(json.dumps({"query": q, "rays": n, "triangles": mesh.triangle_count(), "bvh_width": args.bvh_width,
+                              "elapsed_ms": dt * 1e3, "mrays_per_s": n / dt / 1e6}), flush=True)
     ds.close()
     return 0
 
@@ -120,6 +122,7 @@ def main(argv=None) -> int:
         return adjoint(args, ctx)
     scene, cam = _scene(args)
     ds = ctx.upload(scene)
+    ds.set_bvh_width(args.bvh_width)
     integ = PathIntegrator(args.max_depth, 3)
     env = PYRE_ENV_CDF if args.env_sampling == "cdf" else PYRE_ENV_ALIAS
     film = None

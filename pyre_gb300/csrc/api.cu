@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <thread>
 
 #include "bvh_host.h"
@@ -215,6 +216,7 @@ int pyre_ctx_destroy(pyre_ctx* ctx) {
     if (ctx->render_ws.ptr) cudaFree(ctx->render_ws.ptr);
     if (ctx->io_ws.ptr) cudaFree(ctx->io_ws.ptr);
     if (ctx->tape_ws.ptr) cudaFree(ctx->tape_ws.ptr);
+    if (ctx->prog_ws.ptr) cudaFree(ctx->prog_ws.ptr);
     if (ctx->d_error) cudaFree(ctx->d_error);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     for (auto& ev : ctx->ev)
@@ -514,6 +516,54 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     return PYRE_OK;
 }
 
+namespace pyre {
+
+int select_bvh(pyre_ctx* ctx, pyre_scene* scene, uint32_t requested, DevScene* dev, int* width, bool may_build) {
+    const uint32_t w = requested ? requested : (uint32_t)scene->bvh_width;
+    if (w != 2 && w != 4 && w != 8) return set_error(ctx, PYRE_ERR_INVALID, "bvh_width must be 2, 4 or 8");
+    *dev = scene->dev;
+    *width = (int)w;
+    if (w == 2) return PYRE_OK;
+    pyre_scene::Wide& wd = scene->wide[w == 4 ? 0 : 1];
+    if (!wd.nodes && scene->dev.n_inst > 0) {
+        if (!may_build)
+            return set_error(ctx, PYRE_ERR_INVALID, "the scene has no width-" + std::to_string(w) +
+                                                        " BVH yet (pyre_scene_set_bvh_width builds it)");
+        // collapse from the binary device BVH: one wide BVH per distinct instance BVH
+        std::vector<GpuNode> bin(scene->n_nodes);
+        std::vector<DevInstance> inst(scene->dev.n_inst);
+        PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        PYRE_CUDA_TRY(ctx, cudaMemcpy(bin.data(), scene->dev.nodes, bin.size() * sizeof(GpuNode),
+                                      cudaMemcpyDeviceToHost));
+        PYRE_CUDA_TRY(ctx, cudaMemcpy(inst.data(), scene->dev.inst, inst.size() * sizeof(DevInstance),
+                                      cudaMemcpyDeviceToHost));
+        std::vector<float> flat;
+        std::map<int32_t, int32_t> wide_of;
+        std::vector<int32_t> roots(inst.size(), -1);
+        for (size_t k = 0; k < inst.size(); ++k) {
+            const int32_t r = inst[k].blas_root;
+            if (r < 0) continue;
+            auto it = wide_of.find(r);
+            if (it == wide_of.end()) it = wide_of.emplace(r, collapse_wide(bin, r, (int)w, flat)).first;
+            roots[k] = it->second;
+        }
+        const uint64_t n_wide = flat.size() / ((size_t)PYRE_WIDE_FIELDS * w);
+        if (n_wide * w >= (1ull << 28))
+            return set_error(ctx, PYRE_ERR_UNSUPPORTED, "wide BVH too large for its leaf references");
+        std::vector<float4> nodes4(flat.size() / 4);
+        std::memcpy(nodes4.data(), flat.data(), flat.size() * sizeof(float));
+        int rc = upload(ctx, scene, nodes4, &wd.nodes);
+        if (!rc) rc = upload(ctx, scene, roots, &wd.root);
+        if (rc) { wd.nodes = nullptr; wd.root = nullptr; return rc; }
+        wd.n_nodes = n_wide;
+    }
+    dev->wnodes = wd.nodes;
+    dev->wroot = wd.root;
+    return PYRE_OK;
+}
+
+}  // namespace pyre
+
 extern "C" {
 
 int pyre_scene_upload(pyre_ctx* ctx, const pyre_scene_desc* desc, pyre_scene** out) {
@@ -613,6 +663,18 @@ int pyre_scene_get_info(const pyre_scene* scene, pyre_scene_info* out) {
     out->triangle_bytes = (uint64_t)scene->n_triangles * 48;
     out->node_bytes = scene->n_nodes * 64;
     out->device_bytes = scene->device_bytes;
+    return PYRE_OK;
+}
+
+int pyre_scene_set_bvh_width(pyre_ctx* ctx, pyre_scene* scene, uint32_t width) {
+    if (!ctx || !scene) return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_set_bvh_width: NULL argument");
+    if (width != 2 && width != 4 && width != 8) return set_error(ctx, PYRE_ERR_INVALID, "bvh_width must be 2, 4 or 8");
+    cudaSetDevice(ctx->device);
+    DevScene dev;
+    int w = 2;
+    const int rc = select_bvh(ctx, scene, width, &dev, &w);
+    if (rc) return rc;
+    scene->bvh_width = w;
     return PYRE_OK;
 }
 

@@ -246,6 +246,83 @@ Aabb collapse_bvh2(const pyre_bvh2_node* nodes, uint32_t n_nodes, int32_t node_b
 
 }  // namespace pyre
 
+namespace pyre {
+namespace {
+struct WideChild {
+    Aabb box;
+    int32_t child, count;  // binary node index (count == 0) or leaf slot/count
+};
+inline float half_area(const Aabb& b) {
+    const float dx = b.hi.x - b.lo.x, dy = b.hi.y - b.lo.y, dz = b.hi.z - b.lo.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+inline void binary_children(const GpuNode& g, std::vector<WideChild>& kids) {
+    for (int s = 0; s < 2; ++s) {
+        if (g.d[s] < 0) continue;
+        const float* xy = s == 0 ? g.a : g.b;
+        WideChild c;
+        c.box.lo = mk3(xy[0], xy[2], g.c[2 * s]);
+        c.box.hi = mk3(xy[1], xy[3], g.c[2 * s + 1]);
+        c.child = g.d[s];
+        c.count = g.d[2 + s];
+        kids.push_back(c);
+    }
+}
+}  // namespace
+
+int32_t collapse_wide(const std::vector<GpuNode>& bin, int32_t root, int width, std::vector<float>& out) {
+    const size_t stride = (size_t)PYRE_WIDE_FIELDS * width;
+    // explicit DFS: (binary node, wide slot reserved for it)
+    std::vector<std::pair<int32_t, int32_t>> todo;
+    auto reserve = [&]() {
+        const int32_t w = (int32_t)(out.size() / stride);
+        out.resize(out.size() + stride, 0.0f);
+        return w;
+    };
+    const int32_t wroot = reserve();
+    todo.push_back({root, wroot});
+    std::vector<WideChild> kids;
+    while (!todo.empty()) {
+        const auto [b, w] = todo.back();
+        todo.pop_back();
+        kids.clear();
+        binary_children(bin[(size_t)b], kids);
+        while ((int)kids.size() < width) {
+            int best = -1;
+            float area = -1.0f;
+            for (int k = 0; k < (int)kids.size(); ++k)
+                if (kids[k].count == 0 && half_area(kids[k].box) > area) { area = half_area(kids[k].box); best = k; }
+            if (best < 0) break;
+            const int32_t open = kids[best].child;
+            kids.erase(kids.begin() + best);
+            std::vector<WideChild> grand;
+            binary_children(bin[(size_t)open], grand);
+            kids.insert(kids.begin() + best, grand.begin(), grand.end());
+        }
+        // reserve the interior children first (pre-order: children follow the parent),
+        // pushing them so the first child is expanded next
+        std::vector<int32_t> wide_of(kids.size(), -1);
+        for (size_t k = 0; k < kids.size(); ++k)
+            if (kids[k].count == 0) wide_of[k] = reserve();
+        for (size_t k = kids.size(); k-- > 0;)
+            if (kids[k].count == 0) todo.push_back({kids[k].child, wide_of[k]});
+        float* N = out.data() + (size_t)w * stride;
+        int32_t* I = reinterpret_cast<int32_t*>(N);
+        for (int k = 0; k < width; ++k) {
+            const bool used = k < (int)kids.size();
+            const Aabb bx = used ? kids[k].box : Aabb{splat3(kInf), splat3(-kInf)};
+            N[0 * width + k] = bx.lo.x; N[1 * width + k] = bx.hi.x;
+            N[2 * width + k] = bx.lo.y; N[3 * width + k] = bx.hi.y;
+            N[4 * width + k] = bx.lo.z; N[5 * width + k] = bx.hi.z;
+            I[6 * width + k] = !used ? -1 : (kids[k].count == 0 ? wide_of[k] : kids[k].child);
+            I[7 * width + k] = used ? kids[k].count : 0;
+        }
+    }
+    return wroot;
+}
+
+}  // namespace pyre
+
 extern "C" int pyre_bvh_build(const float* positions, uint32_t n_vertices, const uint32_t* indices,
                               uint32_t n_triangles, pyre_bvh2_node* nodes_out, uint32_t* prim_indices_out,
                               uint32_t* n_nodes_out) {

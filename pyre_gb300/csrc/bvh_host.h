@@ -53,4 +53,25 @@ bool validate_bvh2(const pyre_bvh2_node* nodes, uint32_t n_nodes, const uint32_t
 Aabb collapse_bvh2(const pyre_bvh2_node* nodes, uint32_t n_nodes, int32_t node_base, int32_t slot_base,
                    std::vector<GpuNode>& out);
 
+// Wide device node (W = 4 or 8 children), 32 * W bytes, each field an array
+// over the W child slots so a visit loads whole float4 rows:
+//   lox[W] hix[W] loy[W] hiy[W] loz[W] hiz[W]  child boxes
+//   child[W]  wide node index (count == 0), first triangle slot (count > 0),
+//             -1 for an empty slot
+//   count[W]  triangles of a leaf child, 0 otherwise
+// Stored as a flat float array: field f of child k of node n is element
+// (n * 8 + f) * W + k.
+#ifndef PYRE_WIDE_FIELDS
+#define PYRE_WIDE_FIELDS 8
+#endif
+
+// Collapses the binary device BVH below `root` (a node of `bin`) into wide
+// nodes appended to `out` (8 * W floats each) in depth-first pre-order. Each
+// wide node takes the two children of a binary node and then repeatedly
+// opens the interior child with the largest surface area until it holds W
+// children or only leaves. Boxes, leaves and triangle slots are the binary
+// BVH's own, so a wide traversal tests the same triangles. Returns the wide
+// index of the new root.
+int32_t collapse_wide(const std::vector<GpuNode>& bin, int32_t root, int width, std::vector<float>& out);
+
 }  // namespace pyre

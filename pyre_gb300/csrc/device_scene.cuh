@@ -14,6 +14,10 @@
 #include <cuda_runtime.h>
 #include "pyre_math.cuh"
 
+#ifndef PYRE_WIDE_FIELDS
+#define PYRE_WIDE_FIELDS 8  // fields of a wide node: 6 box planes, child, count
+#endif
+
 namespace pyre {
 
 struct alignas(16) DevInstance {
@@ -73,6 +77,11 @@ struct DevScene {
     const int32_t* part_tlas;    // top-level root per part
     const uint32_t* part_light;  // (first light, light count) per part
     uint32_t n_parts;
+    // wide BVH of the instances (traversals with WIDTH 4 or 8; the top level
+    // stays binary): wide nodes (8 fields x WIDTH floats each) and the wide
+    // root of each instance slot
+    const float4* wnodes;
+    const int32_t* wroot;
 };
 
 struct TraceRay {
@@ -146,6 +155,10 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 //   TOP | n            node of the top-level BVH
 //   INST | slot        enter instance `slot` (root-box test, local origin)
 //   EXIT               leave the current instance (restore the world origin)
+//   LEAF | n*W + k     leaf child k of wide node n (WIDTH > 2)
+// With WIDTH 4 or 8 the instance BVHs are wide: a node step tests every
+// child box, continues with the nearest hit child and pushes the others
+// farthest first; leaf children are parked when they are reached.
 // Inner nodes are stepped while any lane of the warp still needs a leaf; a
 // lane that already holds one leaf keeps stepping speculatively. Leaves found
 // on the way are parked (at most three triangle ranges, all of the current
@@ -158,14 +171,42 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 //            the top-level root to trace; returns the id passed to store
 //   void store(uint32_t id, const TraceRay& r, TraceHit& h, bool found)
 // All 32 lanes of the warp must call trace_stream with the same n and counter.
+#define PYRE_TAG_LEAF (1 << 28)
 #define PYRE_TAG_TOP (1 << 29)
 #define PYRE_TAG_INST (1 << 30)
 #define PYRE_NODE_NONE (-1)
 #define PYRE_NODE_EXIT (-2)
 
-template <bool ANY, class Src>
+// Compare-exchange of (entry distance, stack entry) pairs, ascending.
+__device__ __forceinline__ void cmp_swap(float& ea, int& na, float& eb, int& nb) {
+    const bool sw = eb < ea;
+    const float e = sw ? eb : ea;
+    const int m = sw ? nb : na;
+    eb = sw ? ea : eb;
+    nb = sw ? na : nb;
+    ea = e;
+    na = m;
+}
+template <int W>
+__device__ __forceinline__ void sort_children(float (&e)[W], int (&c)[W]) {
+    if (W == 4) {  // optimal 5-comparator network
+        cmp_swap(e[0], c[0], e[1], c[1]); cmp_swap(e[2], c[2], e[3], c[3]);
+        cmp_swap(e[0], c[0], e[2], c[2]); cmp_swap(e[1], c[1], e[3], c[3]);
+        cmp_swap(e[1], c[1], e[2], c[2]);
+    } else {  // optimal 19-comparator network for 8
+        constexpr int net[19][2] = {{0, 2}, {1, 3}, {4, 6}, {5, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}, {0, 1}, {2, 3},
+                                    {4, 5}, {6, 7}, {2, 4}, {3, 5}, {1, 4}, {3, 6}, {1, 2}, {3, 4}, {5, 6}};
+#pragma unroll
+        for (int q = 0; q < 19; ++q) cmp_swap(e[net[q][0]], c[net[q][0]], e[net[q][1]], c[net[q][1]]);
+    }
+}
+
+template <bool ANY, int WIDTH, class Src>
 __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, uint32_t n, uint32_t* counter,
                                              int refill) {
+    // a lane stops stepping nodes once it holds STOP parked leaves (a binary
+    // step can park two, a wide step at most one)
+    constexpr int STOP = WIDTH > 2 ? 3 : 2;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lanes_below = (1u << lane) - 1u;
@@ -183,7 +224,9 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
     bool found = false;
     bool hit_any = false;    // any-hit: the ray is occluded
     bool exhausted = true;   // no node left to step
-    int stack[PYRE_STACK];
+    // an 8-wide step can push 7 entries, so the 8-wide stack is deeper
+    constexpr int STACK = WIDTH == 8 ? 96 : PYRE_STACK;
+    int stack[STACK];
     int sp = 0;
     int node = PYRE_NODE_NONE;
     int inst = -1;
@@ -235,24 +278,24 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
         }
         // ---- inner phase: step nodes until every lane holds a leaf or has none left
         while (__any_sync(FULL, active && !exhausted && !hit_any && parked == 0)) {
-            if (!active || exhausted || hit_any || parked >= 2) continue;
+            if (!active || exhausted || hit_any || parked >= STOP) continue;
             if (node == PYRE_NODE_NONE) {
                 if (sp == 0) { exhausted = true; continue; }
                 node = stack[--sp];
             }
             if (node == PYRE_NODE_EXIT) {
-                if (parked) { stack[sp++] = PYRE_NODE_EXIT; node = PYRE_NODE_NONE; parked = parked < 2 ? 2 : parked; continue; }
+                if (parked) { stack[sp++] = PYRE_NODE_EXIT; node = PYRE_NODE_NONE; parked = STOP; continue; }
                 inst = -1;
                 o = r.o;
                 node = PYRE_NODE_NONE;
                 continue;
             }
             if (node & PYRE_TAG_INST) {
-                if (parked) { stack[sp++] = node; node = PYRE_NODE_NONE; parked = parked < 2 ? 2 : parked; continue; }
+                if (parked) { stack[sp++] = node; node = PYRE_NODE_NONE; parked = STOP; continue; }
                 const int k = node & ~PYRE_TAG_INST;
                 node = PYRE_NODE_NONE;
                 const DevInstance& I = S.inst[k];
-                const int root = I.blas_root;
+                const int root = WIDTH > 2 ? S.wroot[k] : I.blas_root;
                 if (root < 0) continue;
                 f3 lo = r.o;
                 if (I.has_motion) {
@@ -261,7 +304,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                 }
                 float e;
                 if (!slab(I.lo[0], I.hi[0], I.lo[1], I.hi[1], I.lo[2], I.hi[2], lo, inv, r.tmin, best_t, &e)) continue;
-                if (sp >= PYRE_STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
+                if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                 stack[sp++] = PYRE_NODE_EXIT;
                 inst = k;
                 inst_orig = I.orig_id;
@@ -270,6 +313,52 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                 continue;
             }
             const bool top = (node & PYRE_TAG_TOP) != 0;
+            if (WIDTH > 2 && !top) {
+                if (node & PYRE_TAG_LEAF) {  // park a leaf child of a wide node
+                    const uint32_t ref = (uint32_t)(node & ~PYRE_TAG_LEAF);
+                    const int32_t* NI = reinterpret_cast<const int32_t*>(S.wnodes) +
+                                        (size_t)(ref / WIDTH) * (PYRE_WIDE_FIELDS * WIDTH) + ref % WIDTH;
+                    ls[parked] = __ldg(NI + 6 * WIDTH);
+                    lc[parked] = __ldg(NI + 7 * WIDTH);
+                    ++parked;
+                    node = PYRE_NODE_NONE;
+                    continue;
+                }
+                constexpr int Q = WIDTH / 4;  // float4 rows per field
+                const float4* N = S.wnodes + (size_t)node * (2 * WIDTH);
+                float e[WIDTH];
+                int ent[WIDTH];
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    const float4 lx = __ldg(N + 0 * Q + q), hx = __ldg(N + 1 * Q + q), ly = __ldg(N + 2 * Q + q),
+                                 hy = __ldg(N + 3 * Q + q), lz = __ldg(N + 4 * Q + q), hz = __ldg(N + 5 * Q + q);
+                    const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6 * Q + q));
+                    const int4 ct = __ldg(reinterpret_cast<const int4*>(N + 7 * Q + q));
+                    const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
+                    const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
+                    const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
+                    const int CH[4] = {ch.x, ch.y, ch.z, ch.w}, CT[4] = {ct.x, ct.y, ct.z, ct.w};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        float ek;
+                        const bool h = CH[k] >= 0 && slab(LX[k], HX[k], LY[k], HY[k], LZ[k], HZ[k], o, inv, r.tmin,
+                                                          best_t, &ek);
+                        e[4 * q + k] = h ? ek : __int_as_float(0x7f800000);
+                        ent[4 * q + k] = !h ? PYRE_NODE_NONE
+                                            : (CT[k] > 0 ? (PYRE_TAG_LEAF | (node * WIDTH + 4 * q + k)) : CH[k]);
+                    }
+                }
+                sort_children<WIDTH>(e, ent);
+                int nh = 0;
+#pragma unroll
+                for (int k = 1; k < WIDTH; ++k) nh += ent[k] != PYRE_NODE_NONE ? 1 : 0;
+                if (sp + nh > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
+#pragma unroll
+                for (int k = WIDTH - 1; k >= 1; --k)
+                    if (ent[k] != PYRE_NODE_NONE) stack[sp++] = ent[k];
+                node = ent[0];
+                continue;
+            }
             const float4* N = S.nodes + 4 * (size_t)(node & ~PYRE_TAG_TOP);
             const float4 na = __ldg(N), nb = __ldg(N + 1), nc = __ldg(N + 2);
             const int4 nd = __ldg(reinterpret_cast<const int4*>(N + 3));
@@ -281,7 +370,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
             // leaves: park triangle ranges, or queue the instances of a top-level leaf
             if (top) {
                 const int need = (h0 && leaf0 ? nd.z : 0) + (h1 && leaf1 ? nd.w : 0) + 1;
-                if (sp + need > PYRE_STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
+                if (sp + need > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                 if (h1 && leaf1)
                     for (int k = nd.w - 1; k >= 0; --k) stack[sp++] = PYRE_TAG_INST | (nd.y + k);
                 if (h0 && leaf0)
@@ -294,7 +383,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
             const bool g0 = h0 && !leaf0, g1 = h1 && !leaf1;
             if (g0 && g1) {
                 const bool first0 = e0 <= e1;
-                if (sp >= PYRE_STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
+                if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                 stack[sp++] = (first0 ? nd.y : nd.x) | tag;
                 node = (first0 ? nd.x : nd.y) | tag;
             } else if (g0) {

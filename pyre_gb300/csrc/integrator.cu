@@ -90,6 +90,10 @@ struct WaveParams {
     int smem_grad;       // material gradients summed per block in shared memory
     int refill;          // traversal: idle lanes of a warp that trigger a refetch
     int sort;            // shade reads the live paths sorted by material (P.qsort)
+    int bvh_width;       // instance BVH width of the traversal kernels: 2, 4 or 8
+    // progressive accumulation (pyre_render_progressive): crop npix x 3 running
+    // mean of the radiance, updated once per sample in sample order
+    float* prog_mean;
 };
 
 #define PYRE_DEFAULT_REFILL 16
@@ -271,10 +275,10 @@ struct ExtendRays {
     }
 };
 
-template <bool BATCH>
+template <bool BATCH, int WIDTH>
 __global__ void __launch_bounds__(128) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1]};
-    trace_stream<false>(S, src, P.ctl->count[depth], &P.ctl->fetch[2 * depth], W.refill);
+    trace_stream<false, WIDTH>(S, src, P.ctl->count[depth], &P.ctl->fetch[2 * depth], W.refill);
 }
 
 // ---------------------------------------------------------------- shadow --
@@ -303,10 +307,10 @@ struct ShadowRays {
     }
 };
 
-template <bool BATCH>
+template <bool BATCH, int WIDTH>
 __global__ void __launch_bounds__(128) k_shadow(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ShadowRays<BATCH> src{&S, &P, &W};
-    trace_stream<true>(S, src, P.ctl->scount[depth], &P.ctl->fetch[2 * depth + 1], W.refill);
+    trace_stream<true, WIDTH>(S, src, P.ctl->scount[depth], &P.ctl->fetch[2 * depth + 1], W.refill);
 }
 
 // ------------------------------------------------------- adjoint helpers --
@@ -690,6 +694,9 @@ __global__ void k_accumulate(PathSoA P, WaveParams W) {
     const uint32_t kv = P.ctl->k_valid;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W.npix; p += gridDim.x * blockDim.x) {
         float4 ar = P.acc_r[p], aa = P.acc_a[p], an = P.acc_n[p];
+        f3 mean = splat3(0.0f);
+        if (W.prog_mean && P.ctl->s_base > 0)
+            mean = mk3(W.prog_mean[3 * (size_t)p], W.prog_mean[3 * (size_t)p + 1], W.prog_mean[3 * (size_t)p + 2]);
         for (uint32_t k = 0; k < kv; ++k) {
             uint32_t i = k * W.npix + p;
             float4 Lq = P.L[i];
@@ -697,6 +704,11 @@ __global__ void k_accumulate(PathSoA P, WaveParams W) {
             for (uint32_t s = 0; s < W.ns; ++s) {
                 float4 c = P.pend[(size_t)i * W.ns + s];
                 if (c.w != 0.0f) L = L + mk3(c.x, c.y, c.z);
+            }
+            if (W.prog_mean) {
+                // the viewer's merge of pass s (viewer.rs:164-177): mean += (L - mean) / (s + 1)
+                const float n = (float)(P.ctl->s_base + k + 1);
+                mean = mean + (L - mean) / n;
             }
             float4 a = P.aov_a[i], nn = P.aov_n[i];
             ar.x += L.x; ar.y += L.y; ar.z += L.z; ar.w += a.w;
@@ -706,6 +718,11 @@ __global__ void k_accumulate(PathSoA P, WaveParams W) {
                 P.keep_L[(size_t)(P.ctl->s_base - W.spp_begin + k) * W.npix + p] = make_float4(L.x, L.y, L.z, 0.0f);
         }
         P.acc_r[p] = ar; P.acc_a[p] = aa; P.acc_n[p] = an;
+        if (W.prog_mean) {
+            W.prog_mean[3 * (size_t)p] = mean.x;
+            W.prog_mean[3 * (size_t)p + 1] = mean.y;
+            W.prog_mean[3 * (size_t)p + 2] = mean.z;
+        }
     }
 }
 
@@ -802,12 +819,12 @@ struct QueryRays {
     }
 };
 
-template <bool ANY>
+template <bool ANY, int WIDTH>
 __global__ void __launch_bounds__(128) k_intersect(DevScene S, QueryRays q, uint32_t n, unsigned int* counter,
                                                    int refill) {
     QueryRays src = q;
     src.S = &S;
-    trace_stream<ANY>(S, src, n, counter, refill);
+    trace_stream<ANY, WIDTH>(S, src, n, counter, refill);
 }
 
 // ------------------------------------------------------------ host side --
@@ -875,7 +892,7 @@ struct Launch {
 // block_size (0 = defaults 256/128) sets the shade-type blocks; the trace
 // kernels use min(block_size, 128).
 template <bool BATCH>
-Launch make_launch(pyre_ctx* ctx, uint32_t block_size) {
+Launch make_launch(pyre_ctx* ctx, uint32_t block_size, int width) {
     Launch L;
     if (block_size) {
         const int b = (int)std::max(32u, std::min(256u, block_size / 32 * 32));
@@ -884,8 +901,12 @@ Launch make_launch(pyre_ctx* ctx, uint32_t block_size) {
     }
     L.grid_raygen = grid_for(ctx, k_raygen<BATCH>, L.block_shade);
     L.grid_shade = grid_for(ctx, k_shade<BATCH>, L.block_shade);
-    L.grid_extend = grid_for(ctx, k_extend<BATCH>, L.block_trace);
-    L.grid_shadow = grid_for(ctx, k_shadow<BATCH>, L.block_trace);
+    L.grid_extend = width == 8 ? grid_for(ctx, k_extend<BATCH, 8>, L.block_trace)
+                    : width == 4 ? grid_for(ctx, k_extend<BATCH, 4>, L.block_trace)
+                                 : grid_for(ctx, k_extend<BATCH, 2>, L.block_trace);
+    L.grid_shadow = width == 8 ? grid_for(ctx, k_shadow<BATCH, 8>, L.block_trace)
+                    : width == 4 ? grid_for(ctx, k_shadow<BATCH, 4>, L.block_trace)
+                                 : grid_for(ctx, k_shadow<BATCH, 2>, L.block_trace);
     L.grid_acc = BATCH ? grid_for(ctx, k_accumulate_batch, L.block_shade) : grid_for(ctx, k_accumulate, L.block_shade);
     L.grid_sort = grid_for(ctx, k_sort_scatter, 256);
     return L;
@@ -907,6 +928,22 @@ void mark(pyre_ctx* ctx, int tag) {
 
 enum { STAGE_EXTEND = 0, STAGE_SHADE = 1, STAGE_SHADOW = 2, STAGE_OTHER = 3, STAGE_END = 4 };
 
+// The traversal kernels for the render's BVH width.
+template <bool BATCH>
+void launch_extend(cudaStream_t st, const Launch& Lc, const DevScene& S, const PathSoA& P, const WaveParams& W,
+                   uint32_t d) {
+    if (W.bvh_width == 8) k_extend<BATCH, 8><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
+    else if (W.bvh_width == 4) k_extend<BATCH, 4><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
+    else k_extend<BATCH, 2><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
+}
+template <bool BATCH>
+void launch_shadow(cudaStream_t st, const Launch& Lc, const DevScene& S, const PathSoA& P, const WaveParams& W,
+                   uint32_t d) {
+    if (W.bvh_width == 8) k_shadow<BATCH, 8><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
+    else if (W.bvh_width == 4) k_shadow<BATCH, 4><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
+    else k_shadow<BATCH, 2><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
+}
+
 // Orders the live paths of depth d by shade_key into P.qsort.
 void enqueue_sort(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Launch& Lc, uint32_t d) {
     cudaStream_t st = ctx->stream;
@@ -922,13 +959,13 @@ void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Wave
     k_raygen<false><<<Lc.grid_raygen, Lc.block_shade, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
-        k_extend<false><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
+        launch_extend<false>(st, Lc, S, P, W, d);
         mark(ctx, STAGE_SHADE);
         if (W.sort) enqueue_sort(ctx, S, P, Lc, d);
         k_shade<false><<<Lc.grid_shade, Lc.block_shade, 0, st>>>(S, P, W, d);
         if (W.ns > 0) {
             mark(ctx, STAGE_SHADOW);
-            k_shadow<false><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
+            launch_shadow<false>(st, Lc, S, P, W, d);
         }
     }
     mark(ctx, STAGE_OTHER);
@@ -946,13 +983,13 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
     k_raygen<true><<<Lc.grid_raygen, Lc.block_shade, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
-        k_extend<true><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
+        launch_extend<true>(st, Lc, S, P, W, d);
         mark(ctx, STAGE_SHADE);
         if (W.sort) enqueue_sort(ctx, S, P, Lc, d);
         k_shade<true><<<Lc.grid_shade, Lc.block_shade, 0, st>>>(S, P, W, d);
         if (W.ns > 0) {
             mark(ctx, STAGE_SHADOW);
-            k_shadow<true><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
+            launch_shadow<true>(st, Lc, S, P, W, d);
         }
     }
     mark(ctx, STAGE_OTHER);
@@ -971,7 +1008,7 @@ uint32_t kernels_per_wave(const WaveParams& W) {
 using namespace pyre;
 
 static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
-                       const pyre_render_params* params, pyre_film* film, float4* keep);
+                       const pyre_render_params* params, pyre_film* film, float4* keep, float* prog = nullptr);
 
 extern "C" {
 
@@ -980,12 +1017,41 @@ int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* 
     return render_impl(ctx, scene, camera, params, film, nullptr);
 }
 
+int pyre_render_progressive(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
+                            const pyre_render_params* params, float* mean_rgb, int mem) {
+    if (!ctx || !scene || !camera || !params || !mean_rgb)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_progressive: NULL argument");
+    if (mem != PYRE_MEM_HOST && mem != PYRE_MEM_DEVICE)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_progressive: mem must be PYRE_MEM_HOST or PYRE_MEM_DEVICE");
+    const pyre_render_params& rp = *params;
+    uint32_t x0 = rp.crop[0], y0 = rp.crop[1], x1 = rp.crop[2], y1 = rp.crop[3];
+    if (x0 == 0 && y0 == 0 && x1 == 0 && y1 == 0) { x1 = rp.width; y1 = rp.height; }
+    if (x1 > rp.width || y1 > rp.height || x0 >= x1 || y0 >= y1)
+        return set_error(ctx, PYRE_ERR_INVALID, "crop outside the image");
+    cudaSetDevice(ctx->device);
+    pyre_film none;
+    std::memset(&none, 0, sizeof none);
+    none.mem = PYRE_MEM_DEVICE;
+    if (mem == PYRE_MEM_DEVICE) return render_impl(ctx, scene, camera, params, &none, nullptr, mean_rgb);
+    const size_t bytes = (size_t)(x1 - x0) * (y1 - y0) * 3 * sizeof(float);
+    int rc = ensure_workspace(ctx, ctx->prog_ws, bytes);
+    if (rc) return rc;
+    float* d = (float*)ctx->prog_ws.ptr;
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(d, mean_rgb, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = render_impl(ctx, scene, camera, params, &none, nullptr, d))) return rc;
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(mean_rgb, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return PYRE_OK;
+}
+
 }  // extern "C"
 
 // The render; with `keep` non-null each path's final radiance is also
-// written to keep[(s - spp_begin) * npix + pixel] (pyre_forward).
+// written to keep[(s - spp_begin) * npix + pixel] (pyre_forward). With `prog`
+// non-null (device, crop npix x 3) the samples are merged into that running
+// radiance mean instead of the film's radiance (pyre_render_progressive).
 static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
-                       const pyre_render_params* params, pyre_film* film, float4* keep) {
+                       const pyre_render_params* params, pyre_film* film, float4* keep, float* prog) {
     if (!ctx || !scene || !camera || !params || !film)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_render: NULL argument");
     cudaSetDevice(ctx->device);
@@ -1013,6 +1079,10 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
     W.refill = refill_lanes(&rp);
     W.sort = rp.sort_by_material ? 1 : 0;
+    W.prog_mean = prog;
+    DevScene D;
+    int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width);
+    if (rc) return rc;
     const uint32_t spp = rp.spp_end - rp.spp_begin;
     uint64_t target = rp.wave_paths ? rp.wave_paths : (uint64_t)8 << 20;
     uint64_t K = std::max<uint64_t>(1, target / W.npix);
@@ -1024,14 +1094,14 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
 
     size_t film_bytes = (size_t)W.npix * 10 * sizeof(float);
     size_t need = carve_paths(nullptr, P, std::max(W.ns, 1u), W.npix, nullptr);
-    int rc = ensure_workspace(ctx, ctx->render_ws, need);
+    rc = ensure_workspace(ctx, ctx->render_ws, need);
     if (rc) return rc;
     PathSoA S;
     carve_paths((char*)ctx->render_ws.ptr, P, std::max(W.ns, 1u), W.npix, &S);
     S.keep_L = keep;
     if (film->mem == PYRE_MEM_HOST && (rc = ensure_workspace(ctx, ctx->io_ws, film_bytes))) return rc;
 
-    const Launch Lc = make_launch<false>(ctx, rp.block_size);
+    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
 
     cudaStream_t st = ctx->stream;
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_r, 0, (size_t)W.npix * sizeof(float4), st));
@@ -1040,14 +1110,14 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
     PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
 
-    const DevScene& D = scene->dev;
     ctx->stage_used = 0;
-    if (rp.use_graph && !ctx->stage_timing && !keep) {
+    if (rp.use_graph && !ctx->stage_timing && !keep && !prog) {
         // One wave captured once per configuration, replayed `waves` times.
         char key[256];
-        std::snprintf(key, sizeof key, "%llu/%p/%u/%u/%u/%u/%u/%u/%u/%u/%d/r%d/s%d", (unsigned long long)scene->serial,
-                      ctx->render_ws.ptr, W.npix, W.k_per_wave, W.max_depth, W.min_rr, W.ns, W.spp_begin, W.spp_end,
-                      W.cx0 + W.cy0 * 65536u, W.env_cdf, W.refill, W.sort);
+        std::snprintf(key, sizeof key, "%llu/%p/%u/%u/%u/%u/%u/%u/%u/%u/%d/r%d/s%d/w%d",
+                      (unsigned long long)scene->serial, ctx->render_ws.ptr, W.npix, W.k_per_wave, W.max_depth,
+                      W.min_rr, W.ns, W.spp_begin, W.spp_end, W.cx0 + W.cy0 * 65536u, W.env_cdf, W.refill, W.sort,
+                      W.bvh_width);
         std::string k2 = std::string(key) + "/" + std::to_string(W.width) + "x" + std::to_string(W.height) + "/b" +
                          std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace);
         // camera bytes are part of the key
@@ -1070,7 +1140,7 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     PYRE_CUDA_TRY(ctx, cudaGetLastError());
 
     const float inv_spp = 1.0f / (float)spp;
-    float* out[4] = {film->radiance, film->albedo, film->normal, film->depth};
+    float* out[4] = {prog ? nullptr : film->radiance, film->albedo, film->normal, film->depth};
     float* dst[4];
     float* staging = (float*)ctx->io_ws.ptr;
     size_t offs[4] = {0, (size_t)W.npix * 3, (size_t)W.npix * 6, (size_t)W.npix * 9};
@@ -1190,6 +1260,9 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     W.ns = scene->part_light_max;
     W.refill = refill_lanes(params);
     W.sort = params && params->sort_by_material ? 1 : 0;
+    DevScene D;
+    int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), params ? params->bvh_width : 0u, &D, &W.bvh_width);
+    if (rc) return rc;
     const uint32_t ns = std::max(W.ns, 1u);
 
     // ---- workspace: path state, accumulators, tables, staging film
@@ -1199,7 +1272,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     const size_t stage_bytes = total_pix * 10 * sizeof(float);
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t need = al(path_bytes) + al(job_bytes) + al(seg_bytes) + al(wave_bytes) + al(stage_bytes);
-    int rc = ensure_workspace(ctx, ctx->render_ws, need);
+    rc = ensure_workspace(ctx, ctx->render_ws, need);
     if (rc) return rc;
     char* base = (char*)ctx->render_ws.ptr;
     PathSoA S;
@@ -1219,7 +1292,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_n, 0, total_pix * sizeof(float4), st));
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
 
-    const Launch Lc = make_launch<true>(ctx, params ? params->block_size : 0u);
+    const Launch Lc = make_launch<true>(ctx, params ? params->block_size : 0u, W.bvh_width);
 
     PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
     ctx->stage_used = 0;
@@ -1230,13 +1303,14 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
                           std::to_string((uintptr_t)ctx->render_ws.ptr) + "/" + std::to_string(n_waves) + "/" +
                           std::to_string(max_depth) + "/" + std::to_string(max_paths) + "/b" +
                           std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace) + "/r" +
-                          std::to_string(W.refill) + "/s" + std::to_string(W.sort) + "/";
+                          std::to_string(W.refill) + "/s" + std::to_string(W.sort) + "/w" + std::to_string(W.bvh_width) +
+                          "/";
         key.append(reinterpret_cast<const char*>(dj.data()), job_bytes);
         if (!ctx->wave_graph || ctx->wave_graph_key != key) {
             if (ctx->wave_graph) { cudaGraphExecDestroy(ctx->wave_graph); ctx->wave_graph = nullptr; }
             cudaGraph_t g;
             PYRE_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            for (uint32_t w = 0; w < n_waves; ++w) enqueue_wave_batch(ctx, scene->dev, S, W, Lc);
+            for (uint32_t w = 0; w < n_waves; ++w) enqueue_wave_batch(ctx, D, S, W, Lc);
             PYRE_CUDA_TRY(ctx, cudaStreamEndCapture(st, &g));
             cudaError_t e = cudaGraphInstantiate(&ctx->wave_graph, g, 0);
             cudaGraphDestroy(g);
@@ -1245,7 +1319,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
         }
         PYRE_CUDA_TRY(ctx, cudaGraphLaunch(ctx->wave_graph, st));
     } else {
-        for (uint32_t w = 0; w < n_waves; ++w) enqueue_wave_batch(ctx, scene->dev, S, W, Lc);
+        for (uint32_t w = 0; w < n_waves; ++w) enqueue_wave_batch(ctx, D, S, W, Lc);
     }
     PYRE_CUDA_TRY(ctx, cudaGetLastError());
     k_finalize_batch<<<Lc.grid_acc, 256, 0, st>>>(S, d_jobs, n_jobs, (uint32_t)total_pix, d_stage);
@@ -1334,6 +1408,9 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
     W.refill = refill_lanes(&rp);
     W.sort = rp.sort_by_material ? 1 : 0;
+    DevScene D;
+    int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width, false);
+    if (rc) return rc;
     const uint32_t ns = std::max(W.ns, 1u);
     const size_t cap = PYRE_NOALLOC_SCRATCH_BYTES;
     if (carve_paths(nullptr, W.npix, ns, W.npix, nullptr) > cap) {
@@ -1356,17 +1433,12 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     const uint32_t waves = (uint32_t)((spp + K - 1) / K);
 
     void* scratch = nullptr;
-    int rc = noalloc_scratch(ctx, &scratch);
+    rc = noalloc_scratch(ctx, &scratch);
     if (rc) return rc;
     PathSoA S;
     carve_paths((char*)scratch, (size_t)W.npix * K, ns, W.npix, &S);
 
-    Launch Lc;
-    Lc.grid_raygen = grid_for(ctx, k_raygen<false>, 256);
-    Lc.grid_shade = grid_for(ctx, k_shade<false>, 256);
-    Lc.grid_extend = grid_for(ctx, k_extend<false>, 128);
-    Lc.grid_shadow = grid_for(ctx, k_shadow<false>, 128);
-    Lc.grid_acc = grid_for(ctx, k_accumulate, 256);
+    const Launch Lc = make_launch<false>(ctx, 0u, W.bvh_width);
 
     cudaStream_t st = ctx->stream;
     // The array keeps the previous call's contents: clear the sums and counters.
@@ -1377,7 +1449,7 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
     const int timing = ctx->stage_timing;
     ctx->stage_timing = 0;  // stage timing would create events
-    for (uint32_t w = 0; w < waves; ++w) enqueue_wave(ctx, scene->dev, S, W, Lc);
+    for (uint32_t w = 0; w < waves; ++w) enqueue_wave(ctx, D, S, W, Lc);
     ctx->stage_timing = timing;
     PYRE_CUDA_TRY(ctx, cudaGetLastError());
     k_finalize<<<Lc.grid_acc, 256, 0, st>>>(S, W.npix, 1.0f / (float)spp, film->radiance, film->albedo, film->normal,
@@ -1399,6 +1471,21 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     return PYRE_OK;
 }
 
+template <bool ANY>
+static void launch_intersect(pyre_ctx* ctx, const DevScene& D, const QueryRays& q, uint32_t n, int width) {
+    cudaStream_t st = ctx->stream;
+    if (width == 8) {
+        k_intersect<ANY, 8><<<grid_for(ctx, k_intersect<ANY, 8>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter,
+                                                                                     PYRE_DEFAULT_REFILL);
+    } else if (width == 4) {
+        k_intersect<ANY, 4><<<grid_for(ctx, k_intersect<ANY, 4>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter,
+                                                                                     PYRE_DEFAULT_REFILL);
+    } else {
+        k_intersect<ANY, 2><<<grid_for(ctx, k_intersect<ANY, 2>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter,
+                                                                                     PYRE_DEFAULT_REFILL);
+    }
+}
+
 extern "C" {
 
 static int intersect_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_rays* rays, uint64_t n, pyre_hits* hits,
@@ -1412,6 +1499,9 @@ static int intersect_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_ray
     if (n == 0) return PYRE_OK;
     if (n > 0x7fffffffull) return set_error(ctx, PYRE_ERR_INVALID, "intersect: more than 2^31-1 rays");
     cudaSetDevice(ctx->device);
+    DevScene D;
+    int width = 2;
+    if (int rc0 = select_bvh(ctx, const_cast<pyre_scene*>(scene), 0u, &D, &width)) return rc0;
     cudaStream_t st = ctx->stream;
     const float *org = rays->origin, *dir = rays->direction, *tmin = rays->t_min, *tmax = rays->t_max,
                 *time = rays->time;
@@ -1446,15 +1536,10 @@ static int intersect_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_ray
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), st));
     QueryRays q{};
     q.org = org; q.dir = dir; q.tmin = tmin; q.tmax = tmax; q.time = time;
-    if (any) {
-        q.occluded = occ;
-        int grid = grid_for(ctx, k_intersect<true>, 128);
-        k_intersect<true><<<grid, 128, 0, st>>>(scene->dev, q, (uint32_t)n, ctx->d_counter, PYRE_DEFAULT_REFILL);
-    } else {
-        q.kind = kind; q.inst = inst; q.tri = tri; q.tt = tt; q.uu = uu; q.vv = vv;
-        int grid = grid_for(ctx, k_intersect<false>, 128);
-        k_intersect<false><<<grid, 128, 0, st>>>(scene->dev, q, (uint32_t)n, ctx->d_counter, PYRE_DEFAULT_REFILL);
-    }
+    if (any) q.occluded = occ;
+    else { q.kind = kind; q.inst = inst; q.tri = tri; q.tt = tt; q.uu = uu; q.vv = vv; }
+    if (any) launch_intersect<true>(ctx, D, q, (uint32_t)n, width);
+    else launch_intersect<false>(ctx, D, q, (uint32_t)n, width);
     PYRE_CUDA_TRY(ctx, cudaGetLastError());
     if (mem == PYRE_MEM_HOST) {
         if (any) PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(occluded, occ, n, cudaMemcpyDeviceToHost, st));
@@ -1569,6 +1654,8 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
     W.refill = refill_lanes(&rp);
     W.sort = rp.sort_by_material ? 1 : 0;
+    DevScene D;
+    if ((rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width))) return rc;
     const uint32_t spp = rp.spp_end - rp.spp_begin;
     uint64_t K = std::max<uint64_t>(1, (rp.wave_paths ? rp.wave_paths : (uint64_t)8 << 20) / W.npix);
     K = std::min<uint64_t>(K, spp);
@@ -1608,20 +1695,19 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     const size_t smem = mat_bytes <= 48 * 1024 ? mat_bytes : 0;
     W.smem_grad = smem ? 1 : 0;
 
-    const Launch Lc = make_launch<false>(ctx, rp.block_size);
+    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
     const int grid_adj = grid_for(ctx, k_shade<false, true>, Lc.block_shade, smem);
     const int grid_acc = grid_for(ctx, k_accumulate_adjoint, Lc.block_shade, smem);
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
     PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
-    const DevScene& D = scene->dev;
     for (uint32_t w = 0; w < waves; ++w) {
         k_wave_begin<<<1, 32, 0, st>>>(S.ctl, W.spp_begin, W.spp_end, W.k_per_wave, W.npix);
         k_raygen<false><<<Lc.grid_raygen, Lc.block_shade, 0, st>>>(S, W);
         for (uint32_t d = 0; d < W.max_depth; ++d) {
-            k_extend<false><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(D, S, W, d);
+            launch_extend<false>(st, Lc, D, S, W, d);
             if (W.sort) enqueue_sort(ctx, D, S, Lc, d);
             k_shade<false, true><<<grid_adj, Lc.block_shade, smem, st>>>(D, S, W, d);
-            if (W.ns > 0) k_shadow<false><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(D, S, W, d);
+            if (W.ns > 0) launch_shadow<false>(st, Lc, D, S, W, d);
         }
         k_accumulate_adjoint<<<grid_acc, Lc.block_shade, smem, st>>>(D, S, W);
         k_wave_end<<<1, 32, 0, st>>>(S.ctl, W.max_depth);

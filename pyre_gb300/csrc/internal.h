@@ -18,6 +18,13 @@ struct pyre_scene {
     std::vector<int32_t> part_tlas;    // host copies of the per-part tables
     std::vector<uint32_t> part_light;  // (first, count) per part
     uint64_t device_bytes = 0;
+    // wide BVHs built on first use (index 0: width 4, 1: width 8)
+    struct Wide {
+        float4* nodes = nullptr;
+        int32_t* root = nullptr;  // per instance slot
+        uint64_t n_nodes = 0;
+    } wide[2];
+    int bvh_width = 2;  // traversal width when a call does not choose one
 };
 
 // Reusable device workspace of a context (grown on demand, freed at destroy).
@@ -36,6 +43,7 @@ struct pyre_ctx {
     Workspace render_ws;        // path state of the wavefront integrator
     Workspace io_ws;            // staging for host-memory rays / films
     Workspace tape_ws;          // pyre_forward: per-path radiance for pyre_backward
+    Workspace prog_ws;          // pyre_render_progressive: device copy of a host running mean
     std::string tape_key;       // the render that tape_ws holds
     pyre_render_stats stats{};
     int stage_timing = 0;
@@ -57,6 +65,12 @@ int cuda_check(pyre_ctx* ctx, cudaError_t e, const char* what);
 int ensure_workspace(pyre_ctx* ctx, Workspace& ws, size_t bytes);
 // Reads and clears the kernel error flag; returns its status.
 int take_kernel_error(pyre_ctx* ctx);
+// The scene as the traversal kernels of one call see it: `requested` width
+// (0 = the scene's default) is checked, its wide BVH built if needed, and
+// `dev` gets a copy of the scene with the wide arrays set; *width = 2, 4, 8.
+// With may_build false a wide BVH that does not exist yet is an error.
+int select_bvh(pyre_ctx* ctx, pyre_scene* scene, uint32_t requested, DevScene* dev, int* width,
+               bool may_build = true);
 }  // namespace pyre
 
 #define PYRE_CUDA_TRY(ctx, expr)                                   \

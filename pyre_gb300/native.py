@@ -97,7 +97,7 @@ class RenderParams(C.Structure):
                 ("max_depth", C.c_uint32), ("min_rr_depth", C.c_uint32), ("crop", C.c_uint32 * 4),
                 ("env_sampling", C.c_uint32), ("wave_paths", C.c_uint32), ("block_size", C.c_uint32),
                 ("sort_by_material", C.c_uint32), ("use_graph", C.c_uint32), ("refill_lanes", C.c_uint32),
-                ("reserved", C.c_uint32 * 3)]
+                ("bvh_width", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 class Film(C.Structure):
@@ -136,9 +136,12 @@ SIGNATURES = {
     "pyre_scene_upload": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(C.c_void_p)]),
     "pyre_scene_destroy": (C.c_int, [C.c_void_p, C.c_void_p]),
     "pyre_scene_get_info": (C.c_int, [C.c_void_p, C.POINTER(SceneInfo)]),
+    "pyre_scene_set_bvh_width": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "pyre_intersect_closest": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Rays), C.c_uint64, C.POINTER(Hits), C.c_int]),
     "pyre_intersect_any": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Rays), C.c_uint64, P_u8, C.c_int]),
     "pyre_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams), C.POINTER(Film)]),
+    "pyre_render_progressive": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams),
+                                          C.c_void_p, C.c_int]),
     "pyre_get_render_stats": (C.c_int, [C.c_void_p, C.POINTER(RenderStats)]),
     "pyre_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(CameraDesc), C.POINTER(RenderParams),
                                       C.POINTER(Film)]),

@@ -323,6 +323,10 @@ class DeviceScene:
         N.check(N.load().pyre_scene_get_info(self.handle, C.byref(s)))
         return s
 
+    def set_bvh_width(self, width: int) -> None:
+        """pyre_scene_set_bvh_width: default instance-BVH width (2, 4 or 8)."""
+        self.ctx.check(N.load().pyre_scene_set_bvh_width(self.ctx.handle, self.handle, width))
+
     def close(self):
         if self.handle:
             N.load().pyre_scene_destroy(self.ctx.handle, self.handle)
@@ -366,26 +370,26 @@ class CudaIntegrator:
 
     @staticmethod
     def params(width, height, spp_begin, spp_end, integrator: PathIntegrator, crop=None, env_sampling=0,
-               wave_paths=0, use_graph=0, block_size=0, refill_lanes=0) -> N.RenderParams:
+               wave_paths=0, use_graph=0, block_size=0, refill_lanes=0, bvh_width=0) -> N.RenderParams:
         p = N.RenderParams()
         p.width, p.height, p.spp_begin, p.spp_end = width, height, spp_begin, spp_end
         p.max_depth, p.min_rr_depth = integrator.max_depth, integrator.min_rr_depth
         if crop is not None:
             p.crop[:] = list(crop)
         p.env_sampling, p.wave_paths, p.use_graph, p.block_size = env_sampling, wave_paths, use_graph, block_size
-        p.refill_lanes = refill_lanes
+        p.refill_lanes, p.bvh_width = refill_lanes, bvh_width
         return p
 
     def render(self, dscene: DeviceScene, camera: CameraSpec, integrator: PathIntegrator, width: int, height: int,
                spp: int, spp_begin: int = 0, crop=None, env_sampling: int = 0, wave_paths: int = 0,
-               use_graph: int = 0, refill_lanes: int = 0) -> Film:
+               use_graph: int = 0, refill_lanes: int = 0, bvh_width: int = 0) -> Film:
         """Renders samples [spp_begin, spp_begin+spp) into a (crop-sized) host Film."""
         x0, y0, x1, y1 = crop if crop is not None else (0, 0, width, height)
         film = Film(x1 - x0, y1 - y0)
         f = N.Film(N.fptr(film.radiance), N.fptr(film.albedo), N.fptr(film.normal), N.fptr(film.depth), N.PYRE_MEM_HOST)
         cam = camera.to_desc()
         p = self.params(width, height, spp_begin, spp_begin + spp, integrator, crop, env_sampling, wave_paths, use_graph,
-                        refill_lanes=refill_lanes)
+                        refill_lanes=refill_lanes, bvh_width=bvh_width)
         self.check(self.lib.pyre_render(self.handle, dscene.handle, C.byref(cam), C.byref(p), C.byref(f)))
         return film
 
@@ -398,7 +402,8 @@ class CudaIntegrator:
         return DeviceScene(self, h, scenes)
 
     def render_batch(self, dscene: DeviceScene, jobs: list, wave_paths: int = 0, use_graph: int = 0,
-                     block_size: int = 0, sort_by_material: int = 0, refill_lanes: int = 0) -> list:
+                     block_size: int = 0, sort_by_material: int = 0, refill_lanes: int = 0,
+                     bvh_width: int = 0) -> list:
         """jobs: dicts with part, camera, width, height, spp, spp_begin (0), integrator -> list of Films."""
         films, cjobs = [], []
         for jb in jobs:
@@ -419,9 +424,26 @@ class CudaIntegrator:
         arr = (N.BatchJob * len(cjobs))(*cjobs)
         p = N.RenderParams()
         p.wave_paths, p.use_graph, p.block_size = wave_paths, use_graph, block_size
-        p.sort_by_material, p.refill_lanes = sort_by_material, refill_lanes
+        p.sort_by_material, p.refill_lanes, p.bvh_width = sort_by_material, refill_lanes, bvh_width
         self.check(self.lib.pyre_render_batch(self.handle, dscene.handle, arr, len(cjobs), C.byref(p)))
         return films
+
+    def render_progressive(self, dscene: DeviceScene, camera: CameraSpec, integrator: PathIntegrator, width: int,
+                           height: int, passes: int, mean: np.ndarray | None = None, pass_begin: int = 0,
+                           crop=None, env_sampling: int = 0, **knobs) -> np.ndarray:
+        """pyre_render_progressive: merges passes [pass_begin, pass_begin + passes)
+        (one sample per pixel each) into the running radiance mean (crop h x w x 3
+        float32, updated in place and returned; zeros when None)."""
+        x0, y0, x1, y1 = crop if crop is not None else (0, 0, width, height)
+        if mean is None:
+            mean = np.zeros((y1 - y0, x1 - x0, 3), np.float32)
+        if mean.dtype != np.float32 or not mean.flags.c_contiguous or mean.size != (y1 - y0) * (x1 - x0) * 3:
+            raise ValueError("mean must be a C-contiguous float32 array of crop height x width x 3")
+        cam = camera.to_desc()
+        p = self.params(width, height, pass_begin, pass_begin + passes, integrator, crop, env_sampling, **knobs)
+        self.check(self.lib.pyre_render_progressive(self.handle, dscene.handle, C.byref(cam), C.byref(p),
+                                                    mean.ctypes.data_as(C.c_void_p), N.PYRE_MEM_HOST))
+        return mean
 
     def render_into(self, dscene: DeviceScene, camera: CameraSpec, params: N.RenderParams, film: N.Film) -> None:
         """pyre_render into caller-provided film buffers (host or device pointers)."""

@@ -16,14 +16,15 @@ def _jobs():
     return P.batch_jobs(n_jobs=7, seed=5, resolutions=(32, 48, 64), spps=(1, 3, 4), tri_range=(10, 3000))
 
 
-@pytest.mark.parametrize("use_graph,sort", [(0, 0), (1, 0), (0, 1), (1, 1)])
+@pytest.mark.parametrize("use_graph,sort,width", [(0, 0, 2), (1, 0, 2), (0, 1, 2), (1, 1, 4), (0, 0, 8)])
 @pytest.mark.parametrize("wave_paths", [0, 9000])
-def test_batch_matches_single_renders(gpu_ctx, use_graph, sort, wave_paths):
+def test_batch_matches_single_renders(gpu_ctx, use_graph, sort, width, wave_paths):
     jobs = _jobs()
     ds = gpu_ctx.upload_batch([j["scene"] for j in jobs])
     spec = [{"part": k, "camera": j["camera"], "width": j["width"], "height": j["height"], "spp": j["spp"],
              "integrator": j["integrator"]} for k, j in enumerate(jobs)]
-    films = gpu_ctx.render_batch(ds, spec, wave_paths=wave_paths, use_graph=use_graph, sort_by_material=sort)
+    films = gpu_ctx.render_batch(ds, spec, wave_paths=wave_paths, use_graph=use_graph, sort_by_material=sort,
+                                 bvh_width=width)
     st = gpu_ctx.stats()
     assert st.samples == sum(j["width"] * j["height"] * j["spp"] for j in jobs)
     if wave_paths:

@@ -24,10 +24,12 @@ def _compare(gpu, ref, label):
             f"{label}: {k} not bit-exact, max rel {np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30))}"
 
 
-def test_icosphere_closest_and_any(gpu_ctx, oracle_mod):
+@pytest.mark.parametrize("width", [2, 4, 8])
+def test_icosphere_closest_and_any(gpu_ctx, oracle_mod, width):
     sc = P.microbench_scene(level=6)
     org, d, tmin, tmax = P.random_rays(sc.primitives[0].instance.mesh, 300_000, seed=1)
     ds = gpu_ctx.upload(sc)
+    ds.set_bvh_width(width)
     g = gpu_ctx.intersect(ds, org, d, tmin, tmax)
     osc = oracle_mod.OracleScene(sc)
     r = osc.intersect(org, d, tmin, tmax, canonical=True)
@@ -55,11 +57,13 @@ def _rays_in_box(n, lo, hi, seed, tmax=np.inf):
     return org, d, np.full(n, 1e-4, np.float32), np.full(n, tmax, np.float32)
 
 
+@pytest.mark.parametrize("width", [2, 4, 8])
 @pytest.mark.parametrize("name", ["cornell_box", "cornell_ref"])
-def test_cornell_scenes(gpu_ctx, oracle_mod, name):
+def test_cornell_scenes(gpu_ctx, oracle_mod, name, width):
     sc = getattr(P, name)()
     org, d, tmin, tmax = _rays_in_box(200_000, np.float32(-0.99), np.float32(0.99), seed=5)
     ds = gpu_ctx.upload(sc)
+    ds.set_bvh_width(width)
     g = gpu_ctx.intersect(ds, org, d, tmin, tmax)
     osc = oracle_mod.OracleScene(sc)
     r = osc.intersect(org, d, tmin, tmax)
@@ -71,7 +75,8 @@ def test_cornell_scenes(gpu_ctx, oracle_mod, name):
                           osc.occluded(org, d, np.full_like(tm, 1e-3), tm))
 
 
-def test_motion_blur_instances(gpu_ctx, oracle_mod):
+@pytest.mark.parametrize("width", [2, 4, 8])
+def test_motion_blur_instances(gpu_ctx, oracle_mod, width):
     sc = Scene()
     sc.materials.append(Lambertian([0.5] * 3))
     for k in range(6):
@@ -81,6 +86,7 @@ def test_motion_blur_instances(gpu_ctx, oracle_mod):
     org, d, tmin, tmax = _rays_in_box(200_000, np.array([-2, -1, -1], np.float32), np.array([2, 1, 1], np.float32), 9)
     time = np.random.default_rng(2).random(org.shape[0]).astype(np.float32)
     ds = gpu_ctx.upload(sc)
+    ds.set_bvh_width(width)
     g = gpu_ctx.intersect(ds, org, d, tmin, tmax, time=time)
     r = oracle_mod.OracleScene(sc).intersect(org, d, tmin, tmax, time=time)
     _compare(g, r, "motion")
@@ -99,7 +105,8 @@ def test_caller_supplied_bvh_matches(gpu_ctx, oracle_mod):
     _compare(g, r, "caller BVH")
 
 
-def test_empty_and_degenerate(gpu_ctx, oracle_mod):
+@pytest.mark.parametrize("width", [2, 4, 8])
+def test_empty_and_degenerate(gpu_ctx, oracle_mod, width):
     sc = Scene()
     sc.materials.append(DisneyBsdf([0.5] * 3, 0.0, 0.5))
     # degenerate (zero-area) triangles and coincident centroids
@@ -110,9 +117,18 @@ def test_empty_and_degenerate(gpu_ctx, oracle_mod):
     sc.primitives.append(Primitive(MeshInstance(P.make_uv_sphere((0, 0, 0), 0.5, 8, 4)), 0))
     org, d, tmin, tmax = _rays_in_box(20_000, np.float32(-1), np.float32(1), 11)
     ds = gpu_ctx.upload(sc)
+    ds.set_bvh_width(width)
     _compare(gpu_ctx.intersect(ds, org, d, tmin, tmax), oracle_mod.OracleScene(sc).intersect(org, d, tmin, tmax),
              "degenerate")
     # zero rays
     z = np.zeros((0, 3), np.float32)
     out = gpu_ctx.intersect(ds, z, z, np.zeros(0, np.float32), np.zeros(0, np.float32))
     assert out["kind"].size == 0
+
+
+def test_bvh_width_rejects_bad_values(gpu_ctx):
+    ds = gpu_ctx.upload(P.cornell_box())
+    from pyre_gb300.native import PyreError
+    for w in (0, 3, 16):
+        with pytest.raises(PyreError):
+            ds.set_bvh_width(w)

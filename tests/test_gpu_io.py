@@ -22,8 +22,10 @@ def test_pbrt_cornell_renders_like_the_preset(gpu_ctx, oracle_mod, tmp_path):
     ds_file, ds_code = gpu_ctx.upload(ld.scene), gpu_ctx.upload(sc)
     a = gpu_ctx.render(ds_file, cam, it, 64, 64, 8)
     b = gpu_ctx.render(ds_code, P.cornell_box_camera(64, 64), it, 64, 64, 8)
+    # the loader re-normalizes "normal N" like the reference's builder, which can
+    # move the last bit of the rotated boxes' normals: equal up to that rounding
     for ch in ("radiance", "albedo", "normal", "depth"):
-        np.testing.assert_array_equal(getattr(a, ch), getattr(b, ch))
+        np.testing.assert_allclose(getattr(a, ch), getattr(b, ch), rtol=1e-5, atol=1e-7)
     ref = oracle_mod.OracleScene(ld.scene).render(cam, 64, 64, 8)["radiance"]
     rel = float(np.mean(np.sum((a.radiance - ref) ** 2 / (ref ** 2 + 1e-2), axis=-1)))
     assert rel < 1e-2, rel

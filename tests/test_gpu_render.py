@@ -91,11 +91,13 @@ def test_procedural_studio_small(gpu_ctx, oracle_mod):
     _check(film, ref, bar=1e-2)
 
 
-@pytest.mark.parametrize("refill,sort", [(1, 0), (4, 0), (32, 0), (8, 1), (32, 1)])
-def test_traversal_and_shade_order_do_not_change_results(gpu_ctx, refill, sort):
-    """The traversal kernels refetch rays into finished lanes, and shade can
-    visit the live paths sorted by material; neither the lane, the warp nor
-    the order in which a path is processed may change any bit of the film."""
+@pytest.mark.parametrize("refill,sort,width", [(1, 0, 2), (4, 0, 2), (32, 0, 2), (8, 1, 2), (32, 1, 2), (16, 0, 4),
+                                               (16, 0, 8), (4, 1, 4), (32, 1, 8)])
+def test_traversal_and_shade_order_do_not_change_results(gpu_ctx, refill, sort, width):
+    """The traversal kernels refetch rays into finished lanes, can walk 4- or
+    8-wide instance BVHs, and shade can visit the live paths sorted by
+    material; none of the lane, the warp, the node width or the order in which
+    a path is processed may change any bit of the film."""
     from pyre_gb300 import native as N
     from pyre_gb300.scene import Film
     sc = P.studio_procedural(n_side=3, segments=24, n_moving=2, hdri_size=(256, 128))
@@ -104,7 +106,7 @@ def test_traversal_and_shade_order_do_not_change_results(gpu_ctx, refill, sort):
     it = PathIntegrator(8, 3)
     base = gpu_ctx.render(ds, cam, it, 96, 64, 4)
     film = Film(96, 64)
-    p = gpu_ctx.params(96, 64, 0, 4, it, refill_lanes=refill)
+    p = gpu_ctx.params(96, 64, 0, 4, it, refill_lanes=refill, bvh_width=width)
     p.sort_by_material = sort
     f = N.Film(N.fptr(film.radiance), N.fptr(film.albedo), N.fptr(film.normal), N.fptr(film.depth), N.PYRE_MEM_HOST)
     gpu_ctx.render_into(ds, cam, p, f)
