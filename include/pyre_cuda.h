@@ -69,6 +69,13 @@ typedef struct pyre_bvh2_node {
 int pyre_bvh_build(const float* positions, uint32_t n_vertices, const uint32_t* indices, uint32_t n_triangles,
                    pyre_bvh2_node* nodes_out, uint32_t* prim_indices_out, uint32_t* n_nodes_out);
 
+/* The same build on the GPU of `ctx` (no reference counterpart): the same
+ * nodes, primitive order and node count as pyre_bvh_build, computed level by
+ * level over all open nodes at once. Host arrays in and out. */
+int pyre_bvh_build_device(pyre_ctx* ctx, const float* positions, uint32_t n_vertices, const uint32_t* indices,
+                          uint32_t n_triangles, pyre_bvh2_node* nodes_out, uint32_t* prim_indices_out,
+                          uint32_t* n_nodes_out);
+
 /* -------------------------------------------------------------- Scene --- */
 
 /* TriangleMesh (crates/pyre/src/geometry/mesh.rs:5-11) plus, optionally, the

@@ -22,7 +22,7 @@ LIB = LIB_DIR / "libpyre_cuda.so"
 OBJ_DIR = HERE / "_build"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "integrator.cu", "bvh_host.cpp"]
+SOURCES = ["api.cu", "integrator.cu", "bvh_host.cpp", "bvh_device.cu"]
 HEADERS = ["pyre_math.cuh", "device_scene.cuh", "shading.cuh", "adjoint.cuh", "internal.h", "bvh_host.h"]
 
 

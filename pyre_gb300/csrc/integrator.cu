@@ -275,8 +275,11 @@ struct ExtendRays {
     }
 };
 
+// The traversal kernels ask for 8 resident blocks of 128 threads (at most 64
+// registers, a few bytes of spill): 2 % faster on the 1080p studio frame than
+// the 7 blocks the unconstrained 70-register build allows.
 template <bool BATCH, int WIDTH>
-__global__ void __launch_bounds__(128) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+__global__ void __launch_bounds__(128, 8) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1]};
     trace_stream<false, WIDTH>(S, src, P.ctl->count[depth], &P.ctl->fetch[2 * depth], W.refill);
 }
@@ -308,7 +311,7 @@ struct ShadowRays {
 };
 
 template <bool BATCH, int WIDTH>
-__global__ void __launch_bounds__(128) k_shadow(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+__global__ void __launch_bounds__(128, 8) k_shadow(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ShadowRays<BATCH> src{&S, &P, &W};
     trace_stream<true, WIDTH>(S, src, P.ctl->scount[depth], &P.ctl->fetch[2 * depth + 1], W.refill);
 }

@@ -428,6 +428,19 @@ class CudaIntegrator:
         self.check(self.lib.pyre_render_batch(self.handle, dscene.handle, arr, len(cjobs), C.byref(p)))
         return films
 
+    def bvh_build(self, mesh: TriangleMesh) -> tuple[np.ndarray, np.ndarray]:
+        """pyre_bvh_build_device: the reference BVH of `mesh` built on the GPU
+        (nodes in the Bvh::nodes layout, primitive indices)."""
+        n = mesh.triangle_count()
+        nodes = np.zeros(max(2 * n, 1), N.BVH2_DTYPE)
+        prim = np.zeros(max(n, 1), np.uint32)
+        cnt = C.c_uint32()
+        self.check(self.lib.pyre_bvh_build_device(self.handle, N.fptr(mesh.positions), mesh.positions.shape[0],
+                                                  N.u32ptr(mesh.indices), n,
+                                                  nodes.ctypes.data_as(C.POINTER(N.Bvh2Node)), N.u32ptr(prim),
+                                                  C.byref(cnt)))
+        return nodes[:cnt.value].copy(), prim[:n].copy()
+
     def render_progressive(self, dscene: DeviceScene, camera: CameraSpec, integrator: PathIntegrator, width: int,
                            height: int, passes: int, mean: np.ndarray | None = None, pass_begin: int = 0,
                            crop=None, env_sampling: int = 0, **knobs) -> np.ndarray:
