@@ -145,7 +145,16 @@ def run_batch(args):
     jobs = P.batch_jobs(args.jobs, seed=11)
     gen_s = time.time() - t0
     ctx = CudaIntegrator(0)
+    # scene upload with the instance BVHs built on the host threads, then on the GPU
+    t0 = time.perf_counter()
+    ctx.upload_batch([j["scene"] for j in jobs]).close()
+    upload_host_s = time.perf_counter() - t0
+    ctx.set_bvh_builder("device")
+    ctx.upload_batch([j["scene"] for j in jobs]).close()  # warm-up of the build kernels
+    t0 = time.perf_counter()
     ds = ctx.upload_batch([j["scene"] for j in jobs])
+    upload_device_s = time.perf_counter() - t0
+    ctx.set_bvh_builder("host")
     spec = [{"part": k, "camera": j["camera"], "width": j["width"], "height": j["height"], "spp": j["spp"],
              "integrator": j["integrator"]} for k, j in enumerate(jobs)]
     samples = sum(j["width"] * j["height"] * j["spp"] for j in jobs)
@@ -182,7 +191,9 @@ def run_batch(args):
             "data": "synthetic (seeded Cornell variants)",
             "config": {"workload": f"{args.jobs} jobs, 128^2-1024^2, spp 4/16/64, depth 4-12, inserts 10-200k "
                                    "triangles", "samples": samples, "scene_gen_s": round(gen_s, 1),
-                       "l2": "inputs larger than L2"},
+                       "l2": "inputs larger than L2",
+                       "scene_upload_s": {"host_bvh_build": round(upload_host_s, 3),
+                                          "device_bvh_build": round(upload_device_s, 3)}},
             "per_view_value": samples / v / 1e6, "per_view_ms": v * 1e3, "batched_over_per_view": v / b,
             "autotune": {"best": best, "trials": len(trials)}, "gpu_launches": int(launches),
             "clocks": clk.summary()}

@@ -149,6 +149,14 @@ int pyre_ctx_create(int device, pyre_ctx** out);
 int pyre_ctx_destroy(pyre_ctx* ctx);
 const char* pyre_last_error(const pyre_ctx* ctx);
 
+#define PYRE_BVH_BUILDER_HOST 0   /* build missing mesh BVHs on the host (threads), default */
+#define PYRE_BVH_BUILDER_DEVICE 1 /* build them on the GPU in one pass over all meshes */
+/* Where pyre_scene_upload and pyre_scene_upload_batch build the BVHs of
+ * meshes that come without one. Both give the same BVHs (no reference
+ * counterpart; the reference builds on the host, bvh.rs:45-64). Scenes with a
+ * caller-supplied BVH on any mesh are built on the host. */
+int pyre_set_bvh_builder(pyre_ctx* ctx, int builder);
+
 /* Uploads a flattened scene: collapses each mesh BVH into the device node
  * layout, builds the top-level BVH over instance (swept) bounds and the HDRI
  * sampling tables. */

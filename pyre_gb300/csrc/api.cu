@@ -279,10 +279,14 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     if (desc->env && (desc->env->width == 0 || desc->env->height == 0 || !desc->env->rgb))
         return set_error(ctx, PYRE_ERR_INVALID, "environment map is empty");
 
-    // ---- per-mesh reference BVH2 (caller's, or built here in parallel)
+    // ---- per-mesh reference BVH2 (caller's, or built here in parallel on the
+    // host threads, or built for all meshes at once on the GPU)
+    bool device_build = ctx->bvh_builder == PYRE_BVH_BUILDER_DEVICE;
+    for (uint32_t m = 0; m < n_meshes; ++m)
+        if (desc->meshes[m].bvh_nodes) device_build = false;
     std::vector<std::vector<pyre_bvh2_node>> built(n_meshes);
     std::vector<std::vector<uint32_t>> built_prim(n_meshes);
-    {
+    if (!device_build) {
         std::atomic<uint32_t> next{0};
         auto work = [&]() {
             for (uint32_t m = next++; m < n_meshes; m = next++) {
@@ -322,26 +326,31 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     tris.reserve(3 * total_tris);
     index.reserve(3 * total_tris);
     normal.reserve(3 * total_verts_n);
+    std::vector<uint32_t> device_meshes;  // meshes with triangles, in slot order
     for (uint32_t m = 0; m < n_meshes; ++m) {
         const pyre_mesh_desc& md = desc->meshes[m];
         mesh_index_base[m] = (int32_t)index.size();
         if (md.n_triangles == 0) continue;
-        const pyre_bvh2_node* bn = md.bvh_nodes ? md.bvh_nodes : built[m].data();
-        uint32_t nn = md.bvh_nodes ? md.n_bvh_nodes : (uint32_t)built[m].size();
-        const uint32_t* prim = md.bvh_nodes ? md.bvh_prim_indices : built_prim[m].data();
-        int32_t slot_base = (int32_t)(tris.size() / 3);
-        mesh_root[m] = (int32_t)nodes.size();
-        mesh_box[m] = collapse_bvh2(bn, nn, (int32_t)nodes.size(), slot_base, nodes);
-        for (uint32_t k = 0; k < md.n_triangles; ++k) {
-            uint32_t t = prim[k];
-            const float* p0 = md.positions + 3 * (size_t)md.indices[3 * (size_t)t];
-            const float* p1 = md.positions + 3 * (size_t)md.indices[3 * (size_t)t + 1];
-            const float* p2 = md.positions + 3 * (size_t)md.indices[3 * (size_t)t + 2];
-            float id_bits;
-            std::memcpy(&id_bits, &t, 4);
-            tris.push_back(make_float4(p0[0], p0[1], p0[2], id_bits));
-            tris.push_back(make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.0f));
-            tris.push_back(make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.0f));
+        if (device_build) {
+            device_meshes.push_back(m);
+        } else {
+            const pyre_bvh2_node* bn = md.bvh_nodes ? md.bvh_nodes : built[m].data();
+            uint32_t nn = md.bvh_nodes ? md.n_bvh_nodes : (uint32_t)built[m].size();
+            const uint32_t* prim = md.bvh_nodes ? md.bvh_prim_indices : built_prim[m].data();
+            int32_t slot_base = (int32_t)(tris.size() / 3);
+            mesh_root[m] = (int32_t)nodes.size();
+            mesh_box[m] = collapse_bvh2(bn, nn, (int32_t)nodes.size(), slot_base, nodes);
+            for (uint32_t k = 0; k < md.n_triangles; ++k) {
+                uint32_t t = prim[k];
+                const float* p0 = md.positions + 3 * (size_t)md.indices[3 * (size_t)t];
+                const float* p1 = md.positions + 3 * (size_t)md.indices[3 * (size_t)t + 1];
+                const float* p2 = md.positions + 3 * (size_t)md.indices[3 * (size_t)t + 2];
+                float id_bits;
+                std::memcpy(&id_bits, &t, 4);
+                tris.push_back(make_float4(p0[0], p0[1], p0[2], id_bits));
+                tris.push_back(make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.0f));
+                tris.push_back(make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.0f));
+            }
         }
         uint32_t vbase = md.normals ? (uint32_t)(normal.size() / 3) : 0;
         if (md.normals) {
@@ -350,6 +359,24 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
         }
         for (uint64_t i = 0; i < 3ull * md.n_triangles; ++i) index.push_back(vbase + md.indices[i]);
     }
+
+    // instance BVHs built on the GPU: nodes and triangle records stay on the device
+    DeviceBlas blas;
+    struct FreeNodes {  // the device-built nodes until they are copied into the scene
+        DeviceBlas& b;
+        ~FreeNodes() { if (b.nodes) cudaFree(b.nodes); }
+    } free_nodes{blas};
+    if (device_build && !device_meshes.empty()) {
+        const int rc0 = device_build_blas(ctx, desc, device_meshes, &blas);
+        if (rc0) return fail(rc0);
+        sc->allocations.push_back(blas.tris);
+        sc->device_bytes += 3 * total_tris * sizeof(float4);
+        for (size_t k = 0; k < device_meshes.size(); ++k) {
+            mesh_root[device_meshes[k]] = blas.root[k];
+            mesh_box[device_meshes[k]] = blas.box[k];
+        }
+    }
+    const int32_t node_off = (int32_t)blas.n_nodes;  // top-level nodes follow the device-built ones
 
     // ---- instances and one top-level BVH per part over their swept bounds
     std::vector<DevInstance> inst;
@@ -390,8 +417,8 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
         std::vector<uint32_t> tp;
         build_bvh2(ibox, icent, tn, tp);
         const int32_t slot_base = (int32_t)inst.size();
-        part_tlas[part] = (int32_t)nodes.size();
-        collapse_bvh2(tn.data(), (uint32_t)tn.size(), (int32_t)nodes.size(), slot_base, nodes);
+        part_tlas[part] = node_off + (int32_t)nodes.size();
+        collapse_bvh2(tn.data(), (uint32_t)tn.size(), node_off + (int32_t)nodes.size(), slot_base, nodes);
         inst.resize(inst.size() + tp.size());
         for (size_t k = 0; k < tp.size(); ++k) {
             uint32_t i = live[tp[k]];
@@ -459,10 +486,25 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     std::memset(&D, 0, sizeof D);
     int rc;
     GpuNode* d_nodes = nullptr;
-    if ((rc = upload(ctx, sc, nodes, &d_nodes)) != PYRE_OK) return fail(rc);
+    if (blas.nodes) {  // device-built instance BVHs, then the host-built top levels
+        const size_t total = blas.n_nodes + nodes.size();
+        cudaError_t e = cudaMalloc(&d_nodes, total * sizeof(GpuNode));
+        if (e != cudaSuccess) return fail(cuda_check(ctx, e, "cudaMalloc(scene)"));
+        sc->allocations.push_back(d_nodes);
+        sc->device_bytes += total * sizeof(GpuNode);
+        e = cudaMemcpy(d_nodes, blas.nodes, blas.n_nodes * sizeof(GpuNode), cudaMemcpyDeviceToDevice);
+        cudaFree(blas.nodes);
+        blas.nodes = nullptr;
+        if (e == cudaSuccess && !nodes.empty())
+            e = cudaMemcpy(d_nodes + (size_t)node_off, nodes.data(), nodes.size() * sizeof(GpuNode),
+                           cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(cuda_check(ctx, e, "cudaMemcpy(scene)"));
+    } else if ((rc = upload(ctx, sc, nodes, &d_nodes)) != PYRE_OK) {
+        return fail(rc);
+    }
     D.nodes = reinterpret_cast<const float4*>(d_nodes);
-    float4* d_tris = nullptr;
-    if ((rc = upload(ctx, sc, tris, &d_tris)) != PYRE_OK) return fail(rc);
+    float4* d_tris = blas.tris;
+    if (!d_tris && (rc = upload(ctx, sc, tris, &d_tris)) != PYRE_OK) return fail(rc);
     D.tris = d_tris;
     DevInstance* d_inst = nullptr;
     if ((rc = upload(ctx, sc, inst, &d_inst)) != PYRE_OK) return fail(rc);
@@ -511,7 +553,7 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     }
     D.error_flag = ctx->d_error;
     sc->n_triangles = (uint32_t)total_tris;
-    sc->n_nodes = nodes.size();
+    sc->n_nodes = (uint64_t)node_off + nodes.size();
     *out = sc;
     return PYRE_OK;
 }
@@ -681,6 +723,14 @@ int pyre_scene_set_bvh_width(pyre_ctx* ctx, pyre_scene* scene, uint32_t width) {
 int pyre_get_render_stats(const pyre_ctx* ctx, pyre_render_stats* out) {
     if (!ctx || !out) return PYRE_ERR_INVALID;
     *out = ctx->stats;
+    return PYRE_OK;
+}
+
+int pyre_set_bvh_builder(pyre_ctx* ctx, int builder) {
+    if (!ctx) return PYRE_ERR_INVALID;
+    if (builder != PYRE_BVH_BUILDER_HOST && builder != PYRE_BVH_BUILDER_DEVICE)
+        return set_error(ctx, PYRE_ERR_INVALID, "unknown BVH builder");
+    ctx->bvh_builder = builder;
     return PYRE_OK;
 }
 

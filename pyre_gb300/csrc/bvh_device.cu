@@ -519,6 +519,60 @@ __global__ void k_prim_mesh(const uint32_t* __restrict__ mesh_prim_base, uint32_
     }
 }
 
+// 64-byte device nodes (GpuNode, bvh_host.h) of every mesh: interior node v
+// of mesh m becomes node node_base[m] + ifs[v]; a mesh whose root is a leaf
+// gets one node holding that leaf and an empty slot, as collapse_bvh2 does.
+// Leaf children point at triangle slots, which are the build's positions.
+__global__ void k_emit_gpu(const BNode* __restrict__ nodes, uint32_t n_nodes, uint32_t n_meshes,
+                           const uint32_t* __restrict__ ifs, const uint32_t* __restrict__ node_base, GpuNode* out) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_nodes) return;
+    const BNode& nd = nodes[v];
+    const bool root = v < n_meshes;
+    if (nd.left < 0 && !root) return;
+    GpuNode g;
+    auto put = [&](int s, const BNode& c) {
+        float* xy = s == 0 ? g.a : g.b;
+        xy[0] = c.lo[0]; xy[1] = c.hi[0]; xy[2] = c.lo[1]; xy[3] = c.hi[1];
+        g.c[2 * s] = c.lo[2]; g.c[2 * s + 1] = c.hi[2];
+    };
+    if (nd.left < 0) {  // a root leaf
+        put(0, nd);
+        g.d[0] = (int32_t)nd.start; g.d[2] = (int32_t)nd.count;
+        g.b[0] = INFINITY; g.b[1] = -INFINITY; g.b[2] = INFINITY; g.b[3] = -INFINITY;
+        g.c[2] = INFINITY; g.c[3] = -INFINITY;
+        g.d[1] = -1; g.d[3] = 0;
+        out[node_base[nd.mesh]] = g;
+        return;
+    }
+    const int32_t kid[2] = {nd.left, nd.right};
+    for (int s = 0; s < 2; ++s) {
+        const BNode& c = nodes[kid[s]];
+        put(s, c);
+        if (c.left < 0) { g.d[s] = (int32_t)c.start; g.d[2 + s] = (int32_t)c.count; }
+        else { g.d[s] = (int32_t)(node_base[nd.mesh] + ifs[kid[s]]); g.d[2 + s] = 0; }
+    }
+    out[node_base[nd.mesh] + ifs[v]] = g;
+}
+
+// Triangle records in slot (= build position) order: (v0, local triangle id),
+// e1 = v1 - v0, e2 = v2 - v0 (as pyre_scene_upload lays them out).
+__global__ void k_emit_tris(const uint32_t* __restrict__ idx, uint32_t n, const uint32_t* __restrict__ prim_mesh,
+                            const uint32_t* __restrict__ mesh_prim_base, const float* __restrict__ pos,
+                            const uint32_t* __restrict__ vidx, float4* tris) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const uint32_t t = idx[p];
+        const uint32_t local = t - mesh_prim_base[prim_mesh[p]];
+        const uint32_t i0 = vidx[3 * (size_t)t], i1 = vidx[3 * (size_t)t + 1], i2 = vidx[3 * (size_t)t + 2];
+        const float* p0 = pos + 3 * (size_t)i0;
+        const float* p1 = pos + 3 * (size_t)i1;
+        const float* p2 = pos + 3 * (size_t)i2;
+        tris[3 * (size_t)p] = make_float4(p0[0], p0[1], p0[2], __uint_as_float(local));
+        tris[3 * (size_t)p + 1] = make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.0f);
+        tris[3 * (size_t)p + 2] = make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.0f);
+    }
+}
+
 template <typename T>
 struct DevBuf {
     T* p = nullptr;
@@ -644,6 +698,78 @@ static int build_device_bvh(pyre_ctx* ctx, DeviceBvh& B, const std::vector<uint3
     DTRY(cudaMemcpyAsync(B.mesh_inodes.data(), B.isize.p, M * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     DTRY(cudaStreamSynchronize(st));
     DTRY(cudaGetLastError());
+    return PYRE_OK;
+}
+
+int device_build_blas(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::vector<uint32_t>& mesh_ids,
+                      DeviceBlas* out) {
+    cudaStream_t st = ctx->stream;
+    const uint32_t M = (uint32_t)mesh_ids.size();
+    std::vector<uint32_t> prim_base(M);
+    uint64_t n_tri = 0, n_vert = 0;
+    for (uint32_t k = 0; k < M; ++k) {
+        prim_base[k] = (uint32_t)n_tri;
+        n_tri += desc->meshes[mesh_ids[k]].n_triangles;
+        n_vert += desc->meshes[mesh_ids[k]].n_vertices;
+    }
+    if (n_tri >= (1ull << 31) || 3 * n_vert >= (1ull << 32))
+        return set_error(ctx, PYRE_ERR_UNSUPPORTED, "scene too large for the device BVH build");
+    // all meshes' vertices, and their indices rebased to the concatenation
+    std::vector<uint32_t> vidx(3 * n_tri);
+    std::vector<float> pos(3 * n_vert);
+    uint64_t vb = 0, tb = 0;
+    for (uint32_t k = 0; k < M; ++k) {
+        const pyre_mesh_desc& md = desc->meshes[mesh_ids[k]];
+        std::memcpy(pos.data() + 3 * vb, md.positions, 3 * (size_t)md.n_vertices * sizeof(float));
+        for (uint64_t i = 0; i < 3ull * md.n_triangles; ++i) vidx[3 * tb + i] = (uint32_t)(vb + md.indices[i]);
+        vb += md.n_vertices;
+        tb += md.n_triangles;
+    }
+    DeviceBvh B;
+    B.n_prims = (uint32_t)n_tri;
+    B.n_meshes = M;
+    DevBuf<float> d_pos;
+    DevBuf<uint32_t> d_vidx;
+    DTRY(d_pos.alloc(pos.size())); DTRY(d_vidx.alloc(vidx.size()));
+    DTRY(cudaMemcpyAsync(d_pos.p, pos.data(), pos.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    DTRY(cudaMemcpyAsync(d_vidx.p, vidx.data(), vidx.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    DTRY(B.blo.alloc(n_tri)); DTRY(B.bhi.alloc(n_tri)); DTRY(B.cen.alloc(n_tri));
+    k_tri_bounds<<<blocks_for(n_tri), 256, 0, st>>>(d_pos.p, d_vidx.p, (uint32_t)n_tri, B.blo.p, B.bhi.p, B.cen.p);
+    int rc = build_device_bvh(ctx, B, prim_base);
+    if (rc) return rc;
+    // node bases: interior nodes of each mesh (one node for a leaf root)
+    std::vector<uint32_t> node_base(M);
+    uint64_t total = 0;
+    for (uint32_t k = 0; k < M; ++k) {
+        node_base[k] = (uint32_t)total;
+        total += std::max(B.mesh_inodes[k], 1u);
+    }
+    std::vector<BNode> roots(M);
+    DTRY(cudaMemcpyAsync(roots.data(), B.nodes.p, M * sizeof(BNode), cudaMemcpyDeviceToHost, st));
+    DevBuf<uint32_t> d_node_base;
+    DTRY(d_node_base.alloc(M));
+    DTRY(cudaMemcpyAsync(d_node_base.p, node_base.data(), M * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    GpuNode* d_nodes = nullptr;
+    float4* d_tris = nullptr;
+    DTRY(cudaMalloc(&d_nodes, std::max<uint64_t>(total, 1) * sizeof(GpuNode)));
+    cudaError_t e = cudaMalloc(&d_tris, 3 * n_tri * sizeof(float4));
+    if (e != cudaSuccess) { cudaFree(d_nodes); return cuda_check(ctx, e, "cudaMalloc(triangles)"); }
+    k_emit_gpu<<<blocks_for(B.n_nodes), 256, 0, st>>>(B.nodes.p, B.n_nodes, M, B.ifs.p, d_node_base.p, d_nodes);
+    k_emit_tris<<<blocks_for(n_tri), 256, 0, st>>>(B.idx.p, (uint32_t)n_tri, B.prim_mesh.p, B.mesh_prim_base.p,
+                                                    d_pos.p, d_vidx.p, d_tris);
+    e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) { cudaFree(d_nodes); cudaFree(d_tris); return cuda_check(ctx, e, "device BVH emit"); }
+    out->nodes = d_nodes;
+    out->n_nodes = total;
+    out->tris = d_tris;
+    out->root.assign(M, 0);
+    out->box.assign(M, Aabb{});
+    for (uint32_t k = 0; k < M; ++k) {
+        out->root[k] = (int32_t)node_base[k];
+        out->box[k].lo = mk3(roots[k].lo[0], roots[k].lo[1], roots[k].lo[2]);
+        out->box[k].hi = mk3(roots[k].hi[0], roots[k].hi[1], roots[k].hi[2]);
+    }
     return PYRE_OK;
 }
 

@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <string>
 #include <vector>
+#include <vector_types.h>
 #include "pyre_math.cuh"
 #include "../../include/pyre_cuda.h"
 
@@ -73,5 +74,17 @@ Aabb collapse_bvh2(const pyre_bvh2_node* nodes, uint32_t n_nodes, int32_t node_b
 // BVH's own, so a wide traversal tests the same triangles. Returns the wide
 // index of the new root.
 int32_t collapse_wide(const std::vector<GpuNode>& bin, int32_t root, int width, std::vector<float>& out);
+
+// Instance BVHs of a scene built on the GPU (bvh_device.cu): device nodes in
+// the GpuNode layout (each mesh's nodes from root[k], depth-first) and the
+// triangle records of all meshes in slot order, both owned by the caller
+// (cudaFree), plus each mesh's root box.
+struct DeviceBlas {
+    GpuNode* nodes = nullptr;
+    uint64_t n_nodes = 0;
+    float4* tris = nullptr;
+    std::vector<int32_t> root;
+    std::vector<Aabb> box;
+};
 
 }  // namespace pyre

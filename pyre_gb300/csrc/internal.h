@@ -4,6 +4,7 @@
 #include <string>
 #include <vector>
 #include "../../include/pyre_cuda.h"
+#include "bvh_host.h"
 #include "device_scene.cuh"
 
 struct pyre_scene {
@@ -44,6 +45,7 @@ struct pyre_ctx {
     Workspace io_ws;            // staging for host-memory rays / films
     Workspace tape_ws;          // pyre_forward: per-path radiance for pyre_backward
     Workspace prog_ws;          // pyre_render_progressive: device copy of a host running mean
+    int bvh_builder = PYRE_BVH_BUILDER_HOST;  // where pyre_scene_upload builds instance BVHs
     std::string tape_key;       // the render that tape_ws holds
     pyre_render_stats stats{};
     int stage_timing = 0;
@@ -71,6 +73,11 @@ int take_kernel_error(pyre_ctx* ctx);
 // With may_build false a wide BVH that does not exist yet is an error.
 int select_bvh(pyre_ctx* ctx, pyre_scene* scene, uint32_t requested, DevScene* dev, int* width,
                bool may_build = true);
+// Builds the reference BVH of meshes `mesh_ids` (all with triangles, in
+// this order: their triangle slots follow one another) on the GPU and lays
+// out their device nodes and triangle records (bvh_device.cu).
+int device_build_blas(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::vector<uint32_t>& mesh_ids,
+                      DeviceBlas* out);
 }  // namespace pyre
 
 #define PYRE_CUDA_TRY(ctx, expr)                                   \

@@ -29,6 +29,7 @@ PYRE_CAMERA_PINHOLE = 0
 PYRE_CAMERA_THIN_LENS = 1
 PYRE_ENV_ALIAS = 0
 PYRE_ENV_CDF = 1
+PYRE_BVH_BUILDER_HOST, PYRE_BVH_BUILDER_DEVICE = 0, 1
 
 F3 = C.c_float * 3
 P_f = C.POINTER(C.c_float)
@@ -130,6 +131,7 @@ class RenderStats(C.Structure):
 SIGNATURES = {
     "pyre_version": (C.c_int, []),
     "pyre_bvh_build": (C.c_int, [P_f, C.c_uint32, P_u32, C.c_uint32, C.POINTER(Bvh2Node), P_u32, P_u32]),
+    "pyre_set_bvh_builder": (C.c_int, [C.c_void_p, C.c_int]),
     "pyre_bvh_build_device": (C.c_int, [C.c_void_p, P_f, C.c_uint32, P_u32, C.c_uint32, C.POINTER(Bvh2Node), P_u32,
                                         P_u32]),
     "pyre_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),

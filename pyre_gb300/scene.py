@@ -428,6 +428,12 @@ class CudaIntegrator:
         self.check(self.lib.pyre_render_batch(self.handle, dscene.handle, arr, len(cjobs), C.byref(p)))
         return films
 
+    def set_bvh_builder(self, builder: str) -> None:
+        """pyre_set_bvh_builder: "host" (threads) or "device" (one GPU pass over
+        all meshes) for the BVHs that uploads build."""
+        code = {"host": N.PYRE_BVH_BUILDER_HOST, "device": N.PYRE_BVH_BUILDER_DEVICE}[builder]
+        self.check(self.lib.pyre_set_bvh_builder(self.handle, code))
+
     def bvh_build(self, mesh: TriangleMesh) -> tuple[np.ndarray, np.ndarray]:
         """pyre_bvh_build_device: the reference BVH of `mesh` built on the GPU
         (nodes in the Bvh::nodes layout, primitive indices)."""
