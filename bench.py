@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--graph", type=int, default=0, help="replay waves through a CUDA graph")
     ap.add_argument("--bvh-width", type=int, default=0, help="instance BVH width 2, 4 or 8 (0 = 2)")
+    ap.add_argument("--sort", type=int, default=0, help="shade the live paths sorted by material")
     ap.add_argument("--refill", type=int, default=0,
                     help="traversal: idle lanes of a warp that trigger a ray refetch (0 = library default)")
     ap.add_argument("--workload", default="studio", choices=["studio", "batch", "adjoint"],
@@ -342,6 +343,7 @@ def main():
     s0 = rank * SPP
     params = CudaIntegrator.params(W, H, s0, s0 + SPP, integ, env_sampling=N.PYRE_ENV_ALIAS, use_graph=args.graph,
                                     refill_lanes=args.refill, bvh_width=args.bvh_width)
+    params.sort_by_material = args.sort
     npix = W * H
     dev = {k: torch.empty(npix * c, dtype=torch.float32, device="cuda") for k, c in
            (("radiance", 3), ("albedo", 3), ("normal", 3), ("depth", 1))}
@@ -432,7 +434,7 @@ def main():
                        "l2": "inputs larger than L2 (scene %.0f MB + path state)" % (info.device_bytes / 1e6),
                        "triangles": int(info.n_triangles), "scene_gen_s": round(gen_s, 2),
                        "scene_upload_s": round(upload_s, 2), "use_graph": args.graph,
-                       "refill_lanes": args.refill, "bvh_width": args.bvh_width},
+                       "refill_lanes": args.refill, "bvh_width": args.bvh_width, "sort_by_material": args.sort},
             "mrays_per_s": (ext_rays + shadow_rays) * world / t_max / 1e6,
             "rays": {"extend": ext_rays // args.steps, "shadow": shadow_rays // args.steps},
             "wall_s_timed": wall,
