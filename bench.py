@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--graph", type=int, default=0, help="replay waves through a CUDA graph")
     ap.add_argument("--bvh-width", type=int, default=0, help="instance BVH width 2, 4 or 8 (0 = 2)")
     ap.add_argument("--sort", type=int, default=0, help="shade the live paths sorted by material")
+    ap.add_argument("--wave-paths", type=int, default=0, help="paths in flight per wave (0 = library default)")
+    ap.add_argument("--block", type=int, default=0, help="threads per block of the stage kernels (0 = default)")
     ap.add_argument("--refill", type=int, default=0,
                     help="traversal: idle lanes of a warp that trigger a ray refetch (0 = library default)")
     ap.add_argument("--workload", default="studio", choices=["studio", "batch", "adjoint"],
@@ -342,7 +344,8 @@ def main():
     # Weak scaling: rank r renders samples [r*64, (r+1)*64) of the frame.
     s0 = rank * SPP
     params = CudaIntegrator.params(W, H, s0, s0 + SPP, integ, env_sampling=N.PYRE_ENV_ALIAS, use_graph=args.graph,
-                                    refill_lanes=args.refill, bvh_width=args.bvh_width)
+                                    refill_lanes=args.refill, bvh_width=args.bvh_width,
+                                    wave_paths=args.wave_paths, block_size=args.block)
     params.sort_by_material = args.sort
     npix = W * H
     dev = {k: torch.empty(npix * c, dtype=torch.float32, device="cuda") for k, c in
@@ -434,7 +437,8 @@ def main():
                        "l2": "inputs larger than L2 (scene %.0f MB + path state)" % (info.device_bytes / 1e6),
                        "triangles": int(info.n_triangles), "scene_gen_s": round(gen_s, 2),
                        "scene_upload_s": round(upload_s, 2), "use_graph": args.graph,
-                       "refill_lanes": args.refill, "bvh_width": args.bvh_width, "sort_by_material": args.sort},
+                       "refill_lanes": args.refill, "bvh_width": args.bvh_width, "sort_by_material": args.sort,
+                       "wave_paths": args.wave_paths, "block_size": args.block},
             "mrays_per_s": (ext_rays + shadow_rays) * world / t_max / 1e6,
             "rays": {"extend": ext_rays // args.steps, "shadow": shadow_rays // args.steps},
             "wall_s_timed": wall,

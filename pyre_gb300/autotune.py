@@ -20,14 +20,14 @@ import os
 from pathlib import Path
 
 KNOBS = {
-    "wave_paths": [2 << 20, 4 << 20, 8 << 20, 16 << 20],
+    "wave_paths": [0, 8 << 20, 32 << 20, 128 << 20],  # 0: the library's memory-based choice
     "block_size": [128, 256],
     "use_graph": [0, 1],
     "bvh_width": [2, 4, 8],
     "sort_by_material": [0, 1],
     "refill_lanes": [4, 8, 16, 32],
 }
-DEFAULT = {"wave_paths": 8 << 20, "block_size": 256, "use_graph": 0, "bvh_width": 2, "sort_by_material": 0,
+DEFAULT = {"wave_paths": 0, "block_size": 256, "use_graph": 0, "bvh_width": 2, "sort_by_material": 0,
            "refill_lanes": 16}
 
 

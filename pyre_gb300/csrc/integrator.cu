@@ -425,7 +425,7 @@ __global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
 // ADJ: the path-replay adjoint of the same vertex (pyre_backward): the same
 // draws and decisions, plus the derivatives of its terms.
 template <bool BATCH, bool ADJ = false>
-__global__ void __launch_bounds__(256) k_shade(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+__global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     extern __shared__ double sgrad[];
     if (ADJ && W.smem_grad) {
         for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x) sgrad[k] = 0.0;
@@ -885,6 +885,24 @@ size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* ou
     return c.off + 256;
 }
 
+// Default wave capacity: the paths whose state fits a quarter of the device
+// memory that is free (counting this context's own path workspace), between
+// 8 Mi and 128 Mi paths. On the 1080p 64-spp studio frame 8, 16, 32, 64 and
+// 128 Mi paths gave 444, 479, 497, 506 and 510 Msamples/s: the last bounces
+// of a wave hold few live paths, and a larger wave spends a smaller share of
+// those launches draining the warps' final rays.
+uint64_t default_wave_paths(pyre_ctx* ctx, uint32_t ns, bool batch, bool adjoint) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return (uint64_t)8 << 20;
+    }
+    const uint64_t per_path =
+        std::max<uint64_t>(1, carve_paths(nullptr, (size_t)1 << 20, std::max(ns, 1u), 0, nullptr, batch, adjoint) >> 20);
+    const uint64_t n = ((uint64_t)free_b + ctx->render_ws.bytes) / 4 / per_path;
+    return std::min<uint64_t>(std::max<uint64_t>(n, (uint64_t)8 << 20), (uint64_t)128 << 20);
+}
+
 struct Launch {
     int block_shade = 256;  // raygen, shade, accumulate (at most 256)
     int block_trace = 128;  // extend, shadow (at most 128)
@@ -1087,7 +1105,7 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width);
     if (rc) return rc;
     const uint32_t spp = rp.spp_end - rp.spp_begin;
-    uint64_t target = rp.wave_paths ? rp.wave_paths : (uint64_t)8 << 20;
+    uint64_t target = rp.wave_paths ? rp.wave_paths : default_wave_paths(ctx, W.ns, false, false);
     uint64_t K = std::max<uint64_t>(1, target / W.npix);
     K = std::min<uint64_t>(K, spp);
     if ((uint64_t)W.npix * K > (uint64_t)1 << 31) K = std::max<uint64_t>(1, ((uint64_t)1 << 31) / W.npix);
@@ -1231,7 +1249,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     if (total_pix > 0x7fffffffull) return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_batch: too many pixels");
 
     // ---- wave plan: jobs packed in order, each job's samples in order
-    uint64_t cap = wave_paths ? wave_paths : (uint64_t)8 << 20;
+    uint64_t cap = wave_paths ? wave_paths : default_wave_paths(ctx, scene->part_light_max, true, false);
     cap = std::min<uint64_t>(std::max<uint64_t>(cap, max_npix), (uint64_t)1 << 31);
     std::vector<DevSeg> segs;
     std::vector<DevWave> waves;
@@ -1660,7 +1678,8 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     DevScene D;
     if ((rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width))) return rc;
     const uint32_t spp = rp.spp_end - rp.spp_begin;
-    uint64_t K = std::max<uint64_t>(1, (rp.wave_paths ? rp.wave_paths : (uint64_t)8 << 20) / W.npix);
+    uint64_t K = std::max<uint64_t>(
+        1, (rp.wave_paths ? rp.wave_paths : default_wave_paths(ctx, W.ns, false, true)) / W.npix);
     K = std::min<uint64_t>(K, spp);
     if ((uint64_t)W.npix * K > (uint64_t)1 << 31) K = std::max<uint64_t>(1, ((uint64_t)1 << 31) / W.npix);
     W.k_per_wave = (uint32_t)K;
