@@ -31,3 +31,24 @@ def test_pbrt_cornell_renders_like_the_preset(gpu_ctx, oracle_mod, tmp_path):
     assert rel < 1e-2, rel
     ds_file.close()
     ds_code.close()
+
+
+def test_cli_scene_file_to_exr_and_progressive_png(tmp_path):
+    """python -m pyre_gb300.cli --scene x.pbrt --output y.exr --aovs all --save-aov-pngs, and --progressive."""
+    from pyre_gb300 import cli, sinks
+    sc = P.cornell_box()
+    f = tmp_path / "cornell.pbrt"
+    f.write_text(scene_to_pbrt(sc, (0, 0, 3), (0, 0, 0), (0, 1, 0), 45, 64, 48))
+    out = tmp_path / "frame.exr"
+    assert cli.main(["--scene", str(f), "--width", "64", "--height", "48", "--spp", "4", "--output", str(out),
+                     "--aovs", "all", "--save-aov-pngs"]) == 0
+    planes = sinks.read_exr(out)
+    assert planes["R"].shape == (48, 64) and "N.Z" in planes and "Z" in planes
+    assert planes["R"].max() > 0
+    for name in ("frame.albedo.png", "frame.normal.png", "frame.depth.png"):
+        assert (tmp_path / name).exists()
+    png = tmp_path / "prog.png"
+    assert cli.main(["--scene", str(f), "--width", "64", "--height", "48", "--spp", "5", "--pass-chunk", "2",
+                     "--progressive", "--output", str(png)]) == 0
+    img = sinks.read_png(png)
+    assert img.shape == (48, 64, 3) and img.max() > 0
