@@ -1,0 +1,78 @@
+"""Edge cases of the render path against the oracle: shallow depths, scenes
+with only an environment or no light at all, large sample indices, one-pixel
+images and crops, and parameters the library must reject."""
+import numpy as np
+import pytest
+
+from pyre_gb300 import presets as P
+from pyre_gb300.native import PYRE_ENV_CDF, PyreError
+from pyre_gb300.scene import HdriEnvironmentLight, Lambertian, MeshInstance, PathIntegrator, Primitive, Scene
+
+pytestmark = pytest.mark.gpu
+
+
+def relmse(x, r):
+    return float(np.mean(np.sum((x - r) ** 2 / (r ** 2 + 1e-2), axis=-1)))
+
+
+@pytest.mark.parametrize("max_depth", [1, 2, 3])
+def test_shallow_depths(gpu_ctx, oracle_mod, max_depth):
+    sc, cam = P.studio_ref(), P.studio_ref_camera(48, 32)
+    ds = gpu_ctx.upload(sc)
+    film = gpu_ctx.render(ds, cam, PathIntegrator(max_depth, 3), 48, 32, 8, env_sampling=PYRE_ENV_CDF)
+    ref = oracle_mod.OracleScene(sc).render(cam, 48, 32, 8, max_depth=max_depth)
+    assert relmse(film.radiance, ref["radiance"]) < 1e-2
+    np.testing.assert_allclose(film.depth, ref["depth"], rtol=1e-3, atol=1e-3)
+
+
+def test_environment_only_scene(gpu_ctx, oracle_mod):
+    sc = Scene()
+    sc.env = HdriEnvironmentLight.gradient((0.2, 0.35, 0.65), (0.95, 0.85, 0.7), 1.5)
+    cam = P.studio_ref_camera(40, 30)
+    ds = gpu_ctx.upload(sc)
+    film = gpu_ctx.render(ds, cam, PathIntegrator(8, 3), 40, 30, 4, env_sampling=PYRE_ENV_CDF)
+    ref = oracle_mod.OracleScene(sc).render(cam, 40, 30, 4)
+    np.testing.assert_allclose(film.radiance, ref["radiance"], rtol=1e-5, atol=1e-6)
+    assert np.all(film.depth == 0) and np.all(film.albedo == 0)
+
+
+def test_scene_without_light_is_black(gpu_ctx, oracle_mod):
+    sc = Scene()
+    sc.materials.append(Lambertian([0.5, 0.5, 0.5]))
+    sc.primitives.append(Primitive(MeshInstance.build(P.make_uv_sphere((0, 0, 0), 0.6, 24, 12)), 0))
+    cam = P.cornell_box_camera(32, 32)
+    ds = gpu_ctx.upload(sc)
+    film = gpu_ctx.render(ds, cam, PathIntegrator(8, 3), 32, 32, 2)
+    ref = oracle_mod.OracleScene(sc).render(cam, 32, 32, 2)
+    assert np.all(film.radiance == 0) and np.all(ref["radiance"] == 0)
+    np.testing.assert_allclose(film.depth, ref["depth"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(film.albedo, ref["albedo"], atol=1e-6)
+
+
+def test_large_sample_index_and_one_pixel(gpu_ctx, oracle_mod):
+    sc, cam = P.cornell_ref(), P.cornell_ref_camera(1, 1)
+    ds = gpu_ctx.upload(sc)
+    osc = oracle_mod.OracleScene(sc)
+    a = gpu_ctx.render(ds, cam, PathIntegrator(8, 3), 1, 1, 64, spp_begin=(1 << 31) - 64)
+    b = osc.render(cam, 1, 1, 64, spp_begin=(1 << 31) - 64)
+    assert relmse(a.radiance, b["radiance"]) < 1e-2
+    cam2 = P.cornell_ref_camera(37, 23)
+    whole = gpu_ctx.render(ds, cam2, PathIntegrator(8, 3), 37, 23, 3)
+    corner = gpu_ctx.render(ds, cam2, PathIntegrator(8, 3), 37, 23, 3, crop=(36, 22, 37, 23))
+    np.testing.assert_array_equal(corner.radiance[0, 0], whole.radiance[22, 36])
+
+
+@pytest.mark.parametrize("kw,match", [
+    ({"width": 0}, "size"),
+    ({"spp": 0}, "sample range"),
+    ({"crop": (0, 0, 40, 10)}, "crop"),
+    ({"crop": (5, 5, 5, 8)}, "crop"),
+    ({"integrator": PathIntegrator(65, 3)}, "max_depth"),
+])
+def test_invalid_parameters_are_rejected(gpu_ctx, kw, match):
+    sc, cam = P.cornell_ref(), P.cornell_ref_camera(32, 16)
+    ds = gpu_ctx.upload(sc)
+    args = dict(width=32, height=16, spp=1, integrator=PathIntegrator(8, 3), crop=None)
+    args.update(kw)
+    with pytest.raises(PyreError, match=match):
+        gpu_ctx.render(ds, cam, args["integrator"], args["width"], args["height"], args["spp"], crop=args["crop"])
