@@ -157,6 +157,13 @@ const char* pyre_last_error(const pyre_ctx* ctx);
  * caller-supplied BVH on any mesh are built on the host. */
 int pyre_set_bvh_builder(pyre_ctx* ctx, int builder);
 
+/* Test support for the error paths (no reference counterpart): after `after`
+ * further device allocations of this context (scene buffers and workspaces),
+ * the next one fails as an out-of-memory would, with PYRE_ERR_OOM, without
+ * touching device memory; -1 disables. The failing call returns the error and
+ * the context stays usable. */
+int pyre_inject_alloc_failure(pyre_ctx* ctx, int after);
+
 /* Uploads a flattened scene: collapses each mesh BVH into the device node
  * layout, builds the top-level BVH over instance (swept) bounds and the HDRI
  * sampling tables. */

@@ -26,6 +26,16 @@ int cuda_check(pyre_ctx* ctx, cudaError_t e, const char* what) {
     return set_error(ctx, e == cudaErrorMemoryAllocation ? PYRE_ERR_OOM : PYRE_ERR_CUDA, msg);
 }
 
+bool injected_alloc_failure(pyre_ctx* ctx) {
+    if (!ctx || ctx->fail_alloc_countdown < 0) return false;
+    if (ctx->fail_alloc_countdown == 0) {
+        ctx->fail_alloc_countdown = -1;
+        return true;
+    }
+    --ctx->fail_alloc_countdown;
+    return false;
+}
+
 int ensure_workspace(pyre_ctx* ctx, Workspace& ws, size_t bytes) {
     if (ws.bytes >= bytes) return PYRE_OK;
     if (ws.ptr) {
@@ -39,10 +49,13 @@ int ensure_workspace(pyre_ctx* ctx, Workspace& ws, size_t bytes) {
         ctx->wave_graph = nullptr;
         ctx->wave_graph_key.clear();
     }
+    if (injected_alloc_failure(ctx))
+        return set_error(ctx, PYRE_ERR_OOM, "cudaMalloc(workspace): injected allocation failure");
     size_t rounded = (bytes + (1u << 20) - 1) & ~(size_t)((1u << 20) - 1);
     cudaError_t e = cudaMalloc(&ws.ptr, rounded);
     if (e != cudaSuccess) {
         ws.ptr = nullptr;
+        cudaGetLastError();  // an allocation failure is not sticky: clear it for the next launch checks
         return cuda_check(ctx, e, "cudaMalloc(workspace)");
     }
     ws.bytes = rounded;
@@ -72,8 +85,13 @@ int upload(pyre_ctx* ctx, pyre_scene* sc, const std::vector<T>& host, T** out) {
     if (host.empty()) return PYRE_OK;
     void* p = nullptr;
     size_t bytes = host.size() * sizeof(T);
+    if (injected_alloc_failure(ctx))
+        return set_error(ctx, PYRE_ERR_OOM, "cudaMalloc(scene): injected allocation failure");
     cudaError_t e = cudaMalloc(&p, bytes);
-    if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(scene)");
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_check(ctx, e, "cudaMalloc(scene)");
+    }
     sc->allocations.push_back(p);
     sc->device_bytes += bytes;
     e = cudaMemcpy(p, host.data(), bytes, cudaMemcpyHostToDevice);
@@ -609,12 +627,14 @@ int select_bvh(pyre_ctx* ctx, pyre_scene* scene, uint32_t requested, DevScene* d
 extern "C" {
 
 int pyre_scene_upload(pyre_ctx* ctx, const pyre_scene_desc* desc, pyre_scene** out) {
+    NvtxRange nvtx("pyre_scene_upload");
     if (!desc) return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_upload: NULL argument");
     std::vector<uint32_t> inst_part(desc->n_instances, 0), light_part(desc->n_lights, 0);
     return upload_parts(ctx, desc, inst_part, light_part, 1, out);
 }
 
 int pyre_scene_upload_batch(pyre_ctx* ctx, const pyre_scene_desc* descs, uint32_t n_parts, pyre_scene** out) {
+    NvtxRange nvtx("pyre_scene_upload_batch");
     if (!ctx || !descs || !out || n_parts == 0)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_scene_upload_batch: NULL argument or no parts");
     std::vector<pyre_mesh_desc> meshes;
@@ -723,6 +743,12 @@ int pyre_scene_set_bvh_width(pyre_ctx* ctx, pyre_scene* scene, uint32_t width) {
 int pyre_get_render_stats(const pyre_ctx* ctx, pyre_render_stats* out) {
     if (!ctx || !out) return PYRE_ERR_INVALID;
     *out = ctx->stats;
+    return PYRE_OK;
+}
+
+int pyre_inject_alloc_failure(pyre_ctx* ctx, int after) {
+    if (!ctx) return PYRE_ERR_INVALID;
+    ctx->fail_alloc_countdown = after < 0 ? -1 : after;
     return PYRE_OK;
 }
 

@@ -780,6 +780,7 @@ using namespace pyre;
 extern "C" int pyre_bvh_build_device(pyre_ctx* ctx, const float* positions, uint32_t n_vertices,
                                      const uint32_t* indices, uint32_t n_triangles, pyre_bvh2_node* nodes_out,
                                      uint32_t* prim_indices_out, uint32_t* n_nodes_out) {
+    NvtxRange nvtx("pyre_bvh_build_device");
     if (!ctx || !positions || !indices || !nodes_out || !prim_indices_out || !n_nodes_out)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_bvh_build_device: NULL argument");
     for (uint64_t i = 0; i < 3ull * n_triangles; ++i)

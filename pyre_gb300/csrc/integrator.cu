@@ -1039,11 +1039,13 @@ extern "C" {
 
 int pyre_render(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
                 const pyre_render_params* params, pyre_film* film) {
+    NvtxRange nvtx("pyre_render");
     return render_impl(ctx, scene, camera, params, film, nullptr);
 }
 
 int pyre_render_progressive(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
                             const pyre_render_params* params, float* mean_rgb, int mem) {
+    NvtxRange nvtx("pyre_render_progressive");
     if (!ctx || !scene || !camera || !params || !mean_rgb)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_progressive: NULL argument");
     if (mem != PYRE_MEM_HOST && mem != PYRE_MEM_DEVICE)
@@ -1211,6 +1213,7 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
 // ----------------------------------------------------------- batch render --
 extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const pyre_batch_job* jobs,
                                  uint32_t n_jobs, const pyre_render_params* params) {
+    NvtxRange nvtx("pyre_render_batch");
     if (!ctx || !scene || !jobs || n_jobs == 0)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_batch: NULL argument or no jobs");
     PYRE_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
@@ -1406,6 +1409,7 @@ int noalloc_scratch(pyre_ctx* ctx, void** out) {
 
 extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
                                    const pyre_render_params* params, pyre_film* film) {
+    NvtxRange nvtx("pyre_render_noalloc");
     if (!ctx || !scene || !camera || !params || !film)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_noalloc: NULL argument");
     PYRE_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
@@ -1515,6 +1519,7 @@ extern "C" {
 
 static int intersect_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_rays* rays, uint64_t n, pyre_hits* hits,
                           uint8_t* occluded, int mem, bool any) {
+    NvtxRange nvtx(any ? "pyre_intersect_any" : "pyre_intersect_closest");
     if (!ctx || !scene || !rays) return set_error(ctx, PYRE_ERR_INVALID, "intersect: NULL argument");
     if (!rays->origin || !rays->direction || !rays->t_min || !rays->t_max)
         return set_error(ctx, PYRE_ERR_INVALID, "intersect: ray arrays missing");
@@ -1633,6 +1638,7 @@ int forward_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc*
 
 extern "C" int pyre_forward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
                             const pyre_render_params* params, pyre_film* film) {
+    NvtxRange nvtx("pyre_forward");
     if (!ctx || !scene || !camera || !params || !film)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_forward: NULL argument");
     return forward_impl(ctx, scene, camera, params, film);
@@ -1641,6 +1647,7 @@ extern "C" int pyre_forward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_c
 extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
                              const pyre_render_params* params, const float* d_loss_d_image, int image_mem,
                              pyre_gradients* grads) {
+    NvtxRange nvtx("pyre_backward");
     if (!ctx || !scene || !camera || !params || !d_loss_d_image || !grads)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_backward: NULL argument");
     PYRE_CUDA_TRY(ctx, cudaSetDevice(ctx->device));

@@ -1,6 +1,7 @@
 // internal.h — context and scene objects behind the C ABI.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <string>
 #include <vector>
 #include "../../include/pyre_cuda.h"
@@ -46,6 +47,7 @@ struct pyre_ctx {
     Workspace tape_ws;          // pyre_forward: per-path radiance for pyre_backward
     Workspace prog_ws;          // pyre_render_progressive: device copy of a host running mean
     int bvh_builder = PYRE_BVH_BUILDER_HOST;  // where pyre_scene_upload builds instance BVHs
+    int64_t fail_alloc_countdown = -1;  // pyre_inject_alloc_failure: allocations until one fails
     std::string tape_key;       // the render that tape_ws holds
     pyre_render_stats stats{};
     int stage_timing = 0;
@@ -65,6 +67,8 @@ int set_error(pyre_ctx* ctx, int code, const std::string& msg);
 int cuda_check(pyre_ctx* ctx, cudaError_t e, const char* what);
 // Grows `ws` to at least `bytes` (contents not preserved).
 int ensure_workspace(pyre_ctx* ctx, Workspace& ws, size_t bytes);
+// True (once) when an injected allocation failure is due (pyre_inject_alloc_failure).
+bool injected_alloc_failure(pyre_ctx* ctx);
 // Reads and clears the kernel error flag; returns its status.
 int take_kernel_error(pyre_ctx* ctx);
 // The scene as the traversal kernels of one call see it: `requested` width
@@ -79,6 +83,15 @@ int select_bvh(pyre_ctx* ctx, pyre_scene* scene, uint32_t requested, DevScene* d
 int device_build_blas(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::vector<uint32_t>& mesh_ids,
                       DeviceBlas* out);
 }  // namespace pyre
+
+// An NVTX range over one public call (visible in nsys / ncu timelines; free
+// when no tool is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 #define PYRE_CUDA_TRY(ctx, expr)                                   \
     do {                                                           \
