@@ -157,6 +157,20 @@ const char* pyre_last_error(const pyre_ctx* ctx);
  * caller-supplied BVH on any mesh are built on the host. */
 int pyre_set_bvh_builder(pyre_ctx* ctx, int builder);
 
+/* Device queries of single components, for known-answer tests of the device
+ * code (no reference counterparts; host arrays in and out).
+ * pyre_distribution2d_query: Distribution2D over width x height `weights`
+ * (distribution.rs:113-172) as the environment light samples it (`mode`
+ * PYRE_ENV_CDF or PYRE_ENV_ALIAS): `samples` gets (u, v, pdf, column, row) for
+ * each of the n draws `u` (2 floats each), `pdfs` the pdf at each of the m
+ * points `uv`. pyre_bsdf_query: for each (wo, u) (3 and 2 floats), `out` gets
+ * 13 floats: sampled (0/1), wi.xyz, f.xyz, pdf from the BSDF's sample, then
+ * eval(wo, wi).xyz and pdf(wo, wi) (material.rs:42-226), and a zero. */
+int pyre_distribution2d_query(pyre_ctx* ctx, const float* weights, uint32_t width, uint32_t height, int mode,
+                              uint32_t n, const float* u, float* samples, uint32_t m, const float* uv, float* pdfs);
+int pyre_bsdf_query(pyre_ctx* ctx, const pyre_material_desc* mat, uint32_t n, const float* wo, const float* u,
+                    float* out);
+
 /* Test support for the error paths (no reference counterpart): after `after`
  * further device allocations of this context (scene buffers and workspaces),
  * the next one fails as an out-of-memory would, with PYRE_ERR_OOM, without

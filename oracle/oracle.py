@@ -36,6 +36,7 @@ _SIG = {
     "orc_bsdf_eval": (None, [P_f, P_f, P_f, C.c_uint32, P_f, P_f]),
     "orc_bsdf_sample": (None, [P_f, P_f, P_f, C.c_uint32, P_u8, P_f, P_f, P_f]),
     "orc_disney_consistency": (C.c_int, [P_f, C.c_uint64, C.c_uint32, P_f, P_f, P_f, P_f]),
+    "orc_disney_draws": (None, [C.c_uint64, C.c_uint32, P_f, P_f]),
     "orc_bvh_build": (C.c_uint32, [P_f, P_u32, C.c_uint32, C.c_void_p, P_u32]),
     "orc_scene_new": (C.c_void_p, []),
     "orc_scene_free": (None, [C.c_void_p]),
@@ -161,6 +162,13 @@ def disney_consistency(mats, seed: int, iters: int):
     vals = [C.c_float() for _ in range(4)]
     n = lib().orc_disney_consistency(_f(p), seed, iters, *[C.byref(v) for v in vals])
     return n, [v.value for v in vals]
+
+
+def disney_draws(seed: int, iters: int):
+    """The (wo, u) inputs of the reference's Disney consistency test, 3 * iters each."""
+    wo, u = np.zeros((3 * iters, 3), F32), np.zeros((3 * iters, 2), F32)
+    lib().orc_disney_draws(seed, iters, _f(wo), _f(u))
+    return wo, u
 
 
 def bvh_build(mesh):

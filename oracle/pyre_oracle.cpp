@@ -1351,6 +1351,22 @@ int orc_disney_consistency(const float* params3x7, uint64_t seed, uint32_t iters
     return count;
 }
 
+// The (wo, u) draws of that test in order (3 * iters of each), for running the
+// same cases through another implementation of the BSDF.
+void orc_disney_draws(uint64_t seed, uint32_t iters, float* wo_out, float* u_out) {
+    Xoshiro256pp rng = Xoshiro256pp::seed_from_u64(seed);
+    for (uint32_t k = 0; k < 3 * iters; ++k) {
+        float cos_t = rng.next_f32() * 0.99f + 0.01f;
+        float phi = rng.next_f32() * TAU;
+        float sin_t = std::sqrt(1.0f - cos_t * cos_t);
+        wo_out[3 * k] = sin_t * std::cos(phi);
+        wo_out[3 * k + 1] = sin_t * std::sin(phi);
+        wo_out[3 * k + 2] = cos_t;
+        u_out[2 * k] = rng.next_f32();
+        u_out[2 * k + 1] = rng.next_f32();
+    }
+}
+
 // ---- BVH build (bvh.rs:45-64): nodes_out must hold 2*ntri nodes -----------
 uint32_t orc_bvh_build(const float* pos, const uint32_t* idx, uint32_t ntri, void* nodes_out, uint32_t* prim_out) {
     Mesh m;

@@ -9,6 +9,7 @@
 
 #include "bvh_host.h"
 #include "internal.h"
+#include "shading.cuh"
 
 namespace pyre {
 
@@ -155,6 +156,27 @@ struct EnvTables {
     std::vector<float2> marg_alias, cond_alias;
 };
 
+// Distribution2D (distribution.rs:113-172) over w x h weights: conditional
+// CDFs per row, marginal CDF over the row integrals, per-bin pdfs, alias tables.
+void build_dist2d(uint32_t w, uint32_t h, const float* weights, EnvTables& t) {
+    t.cond_cdf.resize((size_t)h * (w + 1));
+    t.cond_pdf.resize((size_t)w * h);
+    t.cond_alias.resize((size_t)w * h);
+    std::vector<float> row_integral(h);
+    for (uint32_t y = 0; y < h; ++y) {
+        float* cdf = t.cond_cdf.data() + (size_t)y * (w + 1);
+        row_integral[y] = build_cdf(weights + (size_t)y * w, w, cdf);
+        for (uint32_t x = 0; x < w; ++x) t.cond_pdf[(size_t)y * w + x] = (cdf[x + 1] - cdf[x]) * (float)w;
+        build_alias(cdf, w, t.cond_alias.data() + (size_t)y * w);
+    }
+    t.marg_cdf.resize(h + 1);
+    t.marg_pdf.resize(h);
+    t.marg_alias.resize(h);
+    build_cdf(row_integral.data(), h, t.marg_cdf.data());
+    for (uint32_t y = 0; y < h; ++y) t.marg_pdf[y] = (t.marg_cdf[y + 1] - t.marg_cdf[y]) * (float)h;
+    build_alias(t.marg_cdf.data(), h, t.marg_alias.data());
+}
+
 void build_env_tables(uint32_t w, uint32_t h, const float* rgb, EnvTables& t) {
     t.px.resize((size_t)w * h);
     std::vector<float> weights((size_t)w * h);
@@ -168,22 +190,54 @@ void build_env_tables(uint32_t w, uint32_t h, const float* rgb, EnvTables& t) {
             weights[(size_t)y * w + x] = std::fmax(lum, 0.0f) * sin_theta;
         }
     }
-    t.cond_cdf.resize((size_t)h * (w + 1));
-    t.cond_pdf.resize((size_t)w * h);
-    t.cond_alias.resize((size_t)w * h);
-    std::vector<float> row_integral(h);
-    for (uint32_t y = 0; y < h; ++y) {
-        float* cdf = t.cond_cdf.data() + (size_t)y * (w + 1);
-        row_integral[y] = build_cdf(weights.data() + (size_t)y * w, w, cdf);
-        for (uint32_t x = 0; x < w; ++x) t.cond_pdf[(size_t)y * w + x] = (cdf[x + 1] - cdf[x]) * (float)w;
-        build_alias(cdf, w, t.cond_alias.data() + (size_t)y * w);
+    build_dist2d(w, h, weights.data(), t);
+}
+
+// ------------------------------------------------------ device queries --
+// Distribution2D::sample / pdf (distribution.rs:139-172) through the device
+// code the environment light uses: out_s gets (u, v, pdf, column, row) per
+// draw, out_p the piecewise-constant pdf at each uv.
+__global__ void k_dist2d_query(DevEnv E, int cdf_mode, const float* __restrict__ u, uint32_t n,
+                               const float* __restrict__ uv, uint32_t m, float* out_s, float* out_p) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        float pu, pv, x, y;
+        uint32_t row, col;
+        if (cdf_mode) {
+            y = cdf_sample(E.marg_cdf, E.height, u[2 * i + 1], &pv, &row);
+            x = cdf_sample(E.cond_cdf + (size_t)row * (E.width + 1), E.width, u[2 * i], &pu, &col);
+        } else {
+            y = alias_sample(E.marg_alias, E.marg_pdf, E.height, u[2 * i + 1], &pv, &row);
+            x = alias_sample(E.cond_alias + (size_t)row * E.width, E.cond_pdf + (size_t)row * E.width, E.width,
+                             u[2 * i], &pu, &col);
+        }
+        float* o = out_s + 5 * (size_t)i;
+        o[0] = x; o[1] = y; o[2] = pu * pv; o[3] = (float)col; o[4] = (float)row;
     }
-    t.marg_cdf.resize(h + 1);
-    t.marg_pdf.resize(h);
-    t.marg_alias.resize(h);
-    build_cdf(row_integral.data(), h, t.marg_cdf.data());
-    for (uint32_t y = 0; y < h; ++y) t.marg_pdf[y] = (t.marg_cdf[y + 1] - t.marg_cdf[y]) * (float)h;
-    build_alias(t.marg_cdf.data(), h, t.marg_alias.data());
+    if (i < m) {
+        f2 q; q.x = uv[2 * i]; q.y = uv[2 * i + 1];
+        out_p[i] = env_pdf_uv(E, q);
+    }
+}
+
+// BsdfSample / eval / pdf (material.rs:42-226) per (wo, u): out gets
+// (sampled, wi.xyz, f.xyz, pdf, eval(wo, wi).xyz, pdf(wo, wi)).
+__global__ void k_bsdf_query(Bsdf b, const float* __restrict__ wo, const float* __restrict__ u, uint32_t n,
+                             float* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const f3 w = mk3(wo[3 * (size_t)i], wo[3 * (size_t)i + 1], wo[3 * (size_t)i + 2]);
+    f2 q; q.x = u[2 * (size_t)i]; q.y = u[2 * (size_t)i + 1];
+    f3 wi = splat3(0.0f), f = splat3(0.0f), fe = splat3(0.0f);
+    float pdf = 0.0f, pe = 0.0f;
+    const bool ok = bsdf_sample(b, w, q, &wi, &f, &pdf);
+    if (ok) { fe = bsdf_eval(b, w, wi); pe = bsdf_pdf(b, w, wi); }
+    float* o = out + 13 * (size_t)i;
+    o[0] = ok ? 1.0f : 0.0f;
+    o[1] = wi.x; o[2] = wi.y; o[3] = wi.z;
+    o[4] = f.x; o[5] = f.y; o[6] = f.z; o[7] = pdf;
+    o[8] = fe.x; o[9] = fe.y; o[10] = fe.z; o[11] = pe;
+    o[12] = 0.0f;
 }
 
 std::atomic<uint64_t> g_scene_serial{1};
@@ -743,6 +797,68 @@ int pyre_scene_set_bvh_width(pyre_ctx* ctx, pyre_scene* scene, uint32_t width) {
 int pyre_get_render_stats(const pyre_ctx* ctx, pyre_render_stats* out) {
     if (!ctx || !out) return PYRE_ERR_INVALID;
     *out = ctx->stats;
+    return PYRE_OK;
+}
+
+int pyre_distribution2d_query(pyre_ctx* ctx, const float* weights, uint32_t width, uint32_t height, int mode,
+                              uint32_t n, const float* u, float* samples, uint32_t m, const float* uv, float* pdfs) {
+    if (!ctx || !weights || width == 0 || height == 0 || (n && (!u || !samples)) || (m && (!uv || !pdfs)))
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_distribution2d_query: bad arguments");
+    cudaSetDevice(ctx->device);
+    EnvTables t;
+    build_dist2d(width, height, weights, t);
+    const size_t bytes[] = {t.marg_cdf.size() * 4, t.cond_cdf.size() * 4, t.marg_pdf.size() * 4, t.cond_pdf.size() * 4,
+                            t.marg_alias.size() * 8, t.cond_alias.size() * 8, (size_t)n * 8, (size_t)n * 20,
+                            (size_t)m * 8, (size_t)m * 4};
+    size_t off[11] = {0};
+    for (int k = 0; k < 10; ++k) off[k + 1] = off[k] + ((bytes[k] + 255) & ~(size_t)255);
+    int rc = ensure_workspace(ctx, ctx->io_ws, off[10] + 256);
+    if (rc) return rc;
+    char* b = (char*)ctx->io_ws.ptr;
+    cudaStream_t st = ctx->stream;
+    const void* src[] = {t.marg_cdf.data(), t.cond_cdf.data(), t.marg_pdf.data(), t.cond_pdf.data(),
+                         t.marg_alias.data(), t.cond_alias.data(), u, nullptr, uv, nullptr};
+    for (int k = 0; k < 10; ++k)
+        if (src[k] && bytes[k]) PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(b + off[k], src[k], bytes[k], cudaMemcpyHostToDevice, st));
+    DevEnv E{};
+    E.width = width; E.height = height; E.intensity = 1.0f;
+    E.marg_cdf = (const float*)(b + off[0]); E.cond_cdf = (const float*)(b + off[1]);
+    E.marg_pdf = (const float*)(b + off[2]); E.cond_pdf = (const float*)(b + off[3]);
+    E.marg_alias = (const float2*)(b + off[4]); E.cond_alias = (const float2*)(b + off[5]);
+    const uint32_t threads = std::max(n, m);
+    if (threads)
+        k_dist2d_query<<<(threads + 255) / 256, 256, 0, st>>>(E, mode == PYRE_ENV_CDF ? 1 : 0, (const float*)(b + off[6]), n,
+                                                              (const float*)(b + off[8]), m, (float*)(b + off[7]),
+                                                              (float*)(b + off[9]));
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    if (n) PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(samples, b + off[7], bytes[7], cudaMemcpyDeviceToHost, st));
+    if (m) PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(pdfs, b + off[9], bytes[9], cudaMemcpyDeviceToHost, st));
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    return PYRE_OK;
+}
+
+int pyre_bsdf_query(pyre_ctx* ctx, const pyre_material_desc* mat, uint32_t n, const float* wo, const float* u,
+                    float* out) {
+    if (!ctx || !mat || (n && (!wo || !u || !out)) || mat->kind > PYRE_MAT_DISNEY)
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_bsdf_query: bad arguments");
+    if (n == 0) return PYRE_OK;
+    cudaSetDevice(ctx->device);
+    const size_t b_wo = ((size_t)n * 12 + 255) & ~(size_t)255, b_u = ((size_t)n * 8 + 255) & ~(size_t)255;
+    int rc = ensure_workspace(ctx, ctx->io_ws, b_wo + b_u + (size_t)n * 52 + 256);
+    if (rc) return rc;
+    char* b = (char*)ctx->io_ws.ptr;
+    cudaStream_t st = ctx->stream;
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(b, wo, (size_t)n * 12, cudaMemcpyHostToDevice, st));
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(b + b_wo, u, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    Bsdf bs;
+    bs.kind = mat->kind;
+    bs.base = mk3(mat->base_color[0], mat->base_color[1], mat->base_color[2]);
+    bs.metallic = mat->metallic; bs.roughness = mat->roughness; bs.specular = mat->specular;
+    k_bsdf_query<<<(n + 255) / 256, 256, 0, st>>>(bs, (const float*)b, (const float*)(b + b_wo), n,
+                                                   (float*)(b + b_wo + b_u));
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(out, b + b_wo + b_u, (size_t)n * 52, cudaMemcpyDeviceToHost, st));
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(st));
     return PYRE_OK;
 }
 

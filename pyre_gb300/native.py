@@ -133,6 +133,9 @@ SIGNATURES = {
     "pyre_bvh_build": (C.c_int, [P_f, C.c_uint32, P_u32, C.c_uint32, C.POINTER(Bvh2Node), P_u32, P_u32]),
     "pyre_set_bvh_builder": (C.c_int, [C.c_void_p, C.c_int]),
     "pyre_inject_alloc_failure": (C.c_int, [C.c_void_p, C.c_int]),
+    "pyre_distribution2d_query": (C.c_int, [C.c_void_p, P_f, C.c_uint32, C.c_uint32, C.c_int, C.c_uint32, P_f, P_f,
+                                            C.c_uint32, P_f, P_f]),
+    "pyre_bsdf_query": (C.c_int, [C.c_void_p, C.POINTER(MaterialDesc), C.c_uint32, P_f, P_f, P_f]),
     "pyre_bvh_build_device": (C.c_int, [C.c_void_p, P_f, C.c_uint32, P_u32, C.c_uint32, C.POINTER(Bvh2Node), P_u32,
                                         P_u32]),
     "pyre_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
