@@ -493,18 +493,19 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
         if (code == -1) {
             // Escaped: environment radiance with MIS against the BSDF arm (integrator.rs:243-259).
             if (S.has_env) {
-                f3 le = env_le(S.env, ray_d);
+                const f2 uv = env_dir_to_uv(ray_d);
+                f3 le = env_texture(S.env, uv) * S.env.intensity;
                 if (!is_zero3(le)) {
                     float w_adj = 1.0f;
                     if (last_was_specular) L = L + beta * le;
                     else {
-                        float pdf_env = env_pdf(S.env, ray_d);
+                        float pdf_env = env_pdf_at(S.env, uv);
                         float w = power_heuristic(last_pdf, pdf_env);
                         L = L + beta * le * w;
                         w_adj = w;
                     }
                     // d/d texels of beta * texture(uv) * intensity * w
-                    if (ADJ) scatter_env(S.env, W.env_grad, env_dir_to_uv(ray_d), delta * beta * w_adj);
+                    if (ADJ) scatter_env(S.env, W.env_grad, uv, delta * beta * w_adj);
                 }
             }
         } else if (code <= -2) {
@@ -562,84 +563,51 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
                     const DevJob& J = W.jobs[P.pjob[i]];
                     lfirst = J.light_first; lcount = J.light_count;
                 }
-                // NEE over every quad light (integrator.rs:307-333).
-                for (uint32_t l = 0; l < lcount; ++l) {
-                    f2 ul = g.next_vec2();
-                    const DevQuadLight& Lt = S.lights[lfirst + l];
-                    f3 lpos, lwi;
-                    float lpdf;
-                    if (!quad_sample(Lt, p, ul, &lpos, &lwi, &lpdf)) continue;
-                    if (lpdf <= 0.0f || is_zero3(Lt.emission)) continue;
-                    f3 wi = to_local(fr, lwi);
-                    if (wi.z <= 0.0f) continue;
-                    f3 f = bsdf_eval(mat, wo, wi);
-                    if (is_zero3(f)) continue;
-                    f3 target = lpos - 1e-3f * lwi;
-                    // Scene::occluded (scene.rs:120-140)
-                    f3 tf = target - p_off;
-                    float dist = len3(tf);
-                    float pdf_b = bsdf_pdf(mat, wo, wi);
-                    float w = power_heuristic(lpdf, pdf_b);
-                    f3 contrib = beta * f * Lt.emission * wi.z * w / lpdf;
-                    size_t sidx = (size_t)i * W.ns + l;
-                    P.pend[sidx] = make_float4(contrib.x, contrib.y, contrib.z, 1.0f);
-                    if (ADJ) {  // park d/d params of beta * f * (Le cos w / pdf); cleared if occluded
-                        float gm[6];
-                        jac_dot(mat, wo, wi, delta * beta * (Lt.emission * wi.z * w / lpdf), gm);
-                        float4* G = P.gpend + PYRE_GSLOT * sidx;
-                        G[0] = make_float4(gm[0], gm[1], gm[2], gm[3]);
-                        G[1] = make_float4(gm[4], gm[5], __uint_as_float(I.material), 1.0f);
-                        G[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                // The vertex's sampling arms in the reference's order, each
+                // drawing its two numbers first: NEE for every quad light
+                // (integrator.rs:307-333), NEE for the environment (335-354),
+                // then the BSDF sample (356-387). All three evaluate the BSDF
+                // at one call site, so the kernel holds one copy of it.
+                const uint32_t n_nee = lcount + (S.has_env ? 1u : 0u);
+                for (uint32_t s = 0; s <= n_nee; ++s) {
+                    const f2 u2 = g.next_vec2();
+                    const bool bsdf_arm = s == n_nee, env_arm = !bsdf_arm && s == lcount;
+                    f3 wi, wi_w = splat3(0.0f), le = splat3(0.0f), sh_dir = splat3(0.0f);
+                    float lpdf = 0.0f, sh_tmax = INF;
+                    bool sh_ray = true;
+                    if (bsdf_arm) {
+                        if (!bsdf_sample_dir(mat, wo, u2, &wi)) break;
+                    } else if (!env_arm) {
+                        const DevQuadLight& Lt = S.lights[lfirst + s];
+                        f3 lpos;
+                        if (!quad_sample(Lt, p, u2, &lpos, &wi_w, &lpdf)) continue;
+                        if (lpdf <= 0.0f || is_zero3(Lt.emission)) continue;
+                        wi = to_local(fr, wi_w);
+                        if (wi.z <= 0.0f) continue;
+                        le = Lt.emission;
+                        // Scene::occluded (scene.rs:120-140) towards the light point
+                        const f3 tf = (lpos - 1e-3f * wi_w) - p_off;
+                        const float dist = len3(tf);
+                        sh_ray = dist > 0.0f;
+                        sh_dir = tf / dist;
+                        sh_tmax = dist - 1e-3f;
+                    } else {
+                        env_sample(S.env, u2, W.env_cdf, &wi_w, &le, &lpdf);
+                        if (!(lpdf > 0.0f) || is_zero3(le)) continue;
+                        wi = to_local(fr, wi_w);
+                        if (wi.z <= 0.0f) continue;
+                        sh_dir = wi_w;
                     }
-                    if (dist > 0.0f) {
-                        f3 dir = tf / dist;
-                        P.sh_o[sidx] = make_float4(p_off.x, p_off.y, p_off.z, dist - 1e-3f);
-                        P.sh_d[sidx] = make_float4(dir.x, dir.y, dir.z, time);
-                        P.sq[append_slot(shadow_count)] = (uint32_t)sidx;
-                    }
-                }
-                // Environment NEE arm (integrator.rs:335-354).
-                if (S.has_env) {
-                    f2 ue = g.next_vec2();
-                    f3 ewi, eli;
-                    float epdf;
-                    env_sample(S.env, ue, W.env_cdf, &ewi, &eli, &epdf);
-                    if (epdf > 0.0f && !is_zero3(eli)) {
-                        f3 wi = to_local(fr, ewi);
-                        if (wi.z > 0.0f) {
-                            f3 f = bsdf_eval(mat, wo, wi);
-                            if (!is_zero3(f)) {
-                                float pdf_b = bsdf_pdf(mat, wo, wi);
-                                float w = power_heuristic(epdf, pdf_b);
-                                f3 contrib = beta * f * eli * wi.z * w / epdf;
-                                size_t sidx = (size_t)i * W.ns + S.n_lights;
-                                P.pend[sidx] = make_float4(contrib.x, contrib.y, contrib.z, 1.0f);
-                                if (ADJ) {  // term beta * f * (texture * intensity) * k, k = cos w / pdf
-                                    const float k = wi.z * w / epdf;
-                                    float gm[6];
-                                    jac_dot(mat, wo, wi, delta * beta * (eli * k), gm);
-                                    const f2 uv = env_dir_to_uv(ewi);
-                                    const f3 ke = delta * beta * f * k;
-                                    float4* G = P.gpend + PYRE_GSLOT * sidx;
-                                    G[0] = make_float4(gm[0], gm[1], gm[2], gm[3]);
-                                    G[1] = make_float4(gm[4], gm[5], __uint_as_float(I.material), 1.0f);
-                                    G[2] = make_float4(uv.x, uv.y, 1.0f, 0.0f);
-                                    G[3] = make_float4(ke.x, ke.y, ke.z, 0.0f);
-                                }
-                                P.sh_o[sidx] = make_float4(p_off.x, p_off.y, p_off.z, INF);
-                                P.sh_d[sidx] = make_float4(ewi.x, ewi.y, ewi.z, time);
-                                P.sq[append_slot(shadow_count)] = (uint32_t)sidx;
-                            }
-                        }
-                    }
-                }
-                // BSDF sample, throughput, Russian roulette (integrator.rs:356-375).
-                f3 bwi, bf;
-                float bpdf;
-                if (bsdf_sample(mat, wo, g.next_vec2(), &bwi, &bf, &bpdf) && bpdf > 0.0f) {
-                    float cos_wi = fabsf(bwi.z);
-                    if (cos_wi != 0.0f) {
-                        beta = beta * (bf * cos_wi / bpdf);
+                    f3 f;
+                    float pdf_b;
+                    bsdf_eval_pdf(mat, wo, wi, &f, &pdf_b);
+                    if (bsdf_arm) {
+                        // Bsdf::sample is None for a non-positive Disney pdf;
+                        // the integrator also needs pdf > 0 and cos != 0.
+                        if (!(pdf_b > 0.0f)) break;
+                        const float cos_wi = fabsf(wi.z);
+                        if (cos_wi == 0.0f) break;
+                        beta = beta * (f * cos_wi / pdf_b);
                         bool survive = true;
                         if (depth >= (BATCH ? W.jobs[P.pjob[i]].min_rr : W.min_rr)) {
                             float q = clampf_(1.0f - max_elem3(beta), 0.05f, 0.95f);
@@ -648,17 +616,45 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
                         }
                         if (survive) {
                             // Next ray (integrator.rs:377-387).
-                            f3 nd = to_world(fr, bwi);
+                            f3 nd = to_world(fr, wi);
                             P.ray_o[i] = make_float4(p_off.x, p_off.y, p_off.z, 1e-4f);
                             P.ray_d[i] = make_float4(nd.x, nd.y, nd.z, time);
-                            P.beta[i] = make_float4(beta.x, beta.y, beta.z, bpdf);
+                            P.beta[i] = make_float4(beta.x, beta.y, beta.z, pdf_b);
                             alive = true;
                             if (ADJ) {  // for the next vertex's BSDF-sample gradient
                                 P.brec[3 * (size_t)i] = make_float4(wo.x, wo.y, wo.z, __uint_as_float(I.material));
-                                P.brec[3 * (size_t)i + 1] = make_float4(bwi.x, bwi.y, bwi.z, 1.0f);
-                                P.brec[3 * (size_t)i + 2] = make_float4(bf.x, bf.y, bf.z, 0.0f);
+                                P.brec[3 * (size_t)i + 1] = make_float4(wi.x, wi.y, wi.z, 1.0f);
+                                P.brec[3 * (size_t)i + 2] = make_float4(f.x, f.y, f.z, 0.0f);
                             }
                         }
+                        break;
+                    }
+                    if (is_zero3(f)) continue;
+                    const float w = power_heuristic(lpdf, pdf_b);
+                    const f3 contrib = beta * f * le * wi.z * w / lpdf;
+                    const size_t sidx = (size_t)i * W.ns + (env_arm ? S.n_lights : s);
+                    P.pend[sidx] = make_float4(contrib.x, contrib.y, contrib.z, 1.0f);
+                    if (ADJ) {  // park the slot's d/d params (and texels); cleared if occluded
+                        float4* G = P.gpend + PYRE_GSLOT * sidx;
+                        float gm[6];
+                        if (!env_arm) {  // beta * f * (Le cos w / pdf)
+                            jac_dot(mat, wo, wi, delta * beta * (le * wi.z * w / lpdf), gm);
+                            G[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        } else {  // beta * f * (texture * intensity) * k, k = cos w / pdf
+                            const float k = wi.z * w / lpdf;
+                            jac_dot(mat, wo, wi, delta * beta * (le * k), gm);
+                            const f2 uv = env_dir_to_uv(wi_w);
+                            const f3 ke = delta * beta * f * k;
+                            G[2] = make_float4(uv.x, uv.y, 1.0f, 0.0f);
+                            G[3] = make_float4(ke.x, ke.y, ke.z, 0.0f);
+                        }
+                        G[0] = make_float4(gm[0], gm[1], gm[2], gm[3]);
+                        G[1] = make_float4(gm[4], gm[5], __uint_as_float(I.material), 1.0f);
+                    }
+                    if (sh_ray) {
+                        P.sh_o[sidx] = make_float4(p_off.x, p_off.y, p_off.z, sh_tmax);
+                        P.sh_d[sidx] = make_float4(sh_dir.x, sh_dir.y, sh_dir.z, time);
+                        P.sq[append_slot(shadow_count)] = (uint32_t)sidx;
                     }
                 }
                 store_rng(P.rng, i, g);

@@ -132,6 +132,48 @@ __device__ __forceinline__ float bsdf_pdf(const Bsdf& b, f3 wo, f3 wi) {
     return pd * pdf_d + ps * pdf_s;
 }
 
+// bsdf_eval and bsdf_pdf of the same (wo, wi) in one pass: the half vector,
+// the GGX D term and Lambda(wo) are computed once and shared. Each output
+// goes through the same binary32 operations, in the same order, as the two
+// functions above, so it is bit-identical to them.
+__device__ __forceinline__ void bsdf_eval_pdf(const Bsdf& b, f3 wo, f3 wi, f3* f_out, float* pdf_out) {
+    const bool upper = !(wo.z <= 0.0f || wi.z <= 0.0f);
+    if (b.kind == PYRE_MAT_LAMBERTIAN) {
+        *f_out = upper ? b.base / PYRE_PI : splat3(0.0f);
+        *pdf_out = upper ? wi.z / PYRE_PI : 0.0f;
+        return;
+    }
+    f3 fd = splat3(0.0f), fs = splat3(0.0f);
+    float pdf_s = 0.0f;
+    if (upper) {
+        const f3 h = normalize_or_zero3(wo + wi);
+        if (!(len2(h) < 1e-10f)) {
+            if (!(b.metallic >= 1.0f)) {  // eval_diffuse
+                float cos_d = clampf_(dot3(wi, h), 0.0f, 1.0f);
+                float fd90 = 0.5f + 2.0f * b.roughness * cos_d * cos_d;
+                float fd_v = 1.0f + (fd90 - 1.0f) * powi5(fmaxf(1.0f - wo.z, 0.0f));
+                float fd_l = 1.0f + (fd90 - 1.0f) * powi5(fmaxf(1.0f - wi.z, 0.0f));
+                fd = b.base * (1.0f - b.metallic) / PYRE_PI * fd_v * fd_l;
+            }
+            if (!(h.z <= 0.0f)) {  // eval_specular and pdf_specular
+                const float a = bsdf_alpha(b);
+                const float d = ggx_d(h, a);
+                const float one_lo = 1.0f + ggx_lambda(wo, a);
+                const f3 f = schlick(fmaxf(dot3(wi, h), 0.0f), bsdf_f0(b));
+                const float g = 1.0f / (one_lo + ggx_lambda(wi, a));
+                fs = d * f * g / (4.0f * wo.z * wi.z);
+                const float g1 = 1.0f / one_lo;
+                pdf_s = g1 * d / (4.0f * wo.z);
+            }
+        }
+    }
+    *f_out = fd + fs;
+    float pd, ps;
+    lobe_weights(b, &pd, &ps);
+    const float pdf_d = wi.z <= 0.0f ? 0.0f : wi.z / PYRE_PI;
+    *pdf_out = pd * pdf_d + ps * pdf_s;
+}
+
 __device__ __forceinline__ f3 sample_ggx_vndf(f3 wo, float alpha, f2 u) {  // material.rs:291-317
     f3 vh = normalize3(mk3(alpha * wo.x, alpha * wo.y, wo.z));
     float lensq = vh.x * vh.x + vh.y * vh.y;
@@ -149,17 +191,15 @@ __device__ __forceinline__ f3 sample_ggx_vndf(f3 wo, float alpha, f2 u) {  // ma
     return normalize3(mk3(alpha * nh.x, alpha * nh.y, fmaxf(nh.z, 0.0f)));
 }
 
-// Bsdf::sample (material.rs:68-76 Lambertian, 197-225 Disney).
-__device__ __forceinline__ bool bsdf_sample(const Bsdf& b, f3 wo, f2 u, f3* wi_out, f3* f_out, float* pdf_out) {
+// The direction drawn by Bsdf::sample (material.rs:68-76 Lambertian,
+// 197-222 Disney); false where the reference returns None before it
+// evaluates the pdf. A Lambertian draw always has wi.z > 0 (u.x < 1).
+__device__ __forceinline__ bool bsdf_sample_dir(const Bsdf& b, f3 wo, f2 u, f3* wi_out) {
+    if (wo.z <= 0.0f) return false;
     if (b.kind == PYRE_MAT_LAMBERTIAN) {
-        if (wo.z <= 0.0f) return false;
-        f3 wi = cosine_sample_hemisphere(u);
-        *wi_out = wi;
-        *pdf_out = wi.z / PYRE_PI;
-        *f_out = b.base / PYRE_PI;
+        *wi_out = cosine_sample_hemisphere(u);
         return true;
     }
-    if (wo.z <= 0.0f) return false;
     float pd, ps;
     lobe_weights(b, &pd, &ps);
     if (pd + ps <= 0.0f) return false;
@@ -173,10 +213,21 @@ __device__ __forceinline__ bool bsdf_sample(const Bsdf& b, f3 wo, f2 u, f3* wi_o
         wi = 2.0f * dot3(wo, h) * h - wo;  // reflect, material.rs:285-287
     }
     if (wi.z <= 0.0f) return false;
-    float p = bsdf_pdf(b, wo, wi);
-    if (p <= 0.0f) return false;
     *wi_out = wi;
-    *f_out = bsdf_eval(b, wo, wi);
+    return true;
+}
+
+// Bsdf::sample (material.rs:68-76, 197-225): the drawn direction with
+// eval and pdf there; None where the pdf is not positive (Disney).
+__device__ __forceinline__ bool bsdf_sample(const Bsdf& b, f3 wo, f2 u, f3* wi_out, f3* f_out, float* pdf_out) {
+    f3 wi;
+    if (!bsdf_sample_dir(b, wo, u, &wi)) return false;
+    f3 f;
+    float p;
+    bsdf_eval_pdf(b, wo, wi, &f, &p);
+    if (b.kind != PYRE_MAT_LAMBERTIAN && p <= 0.0f) return false;
+    *wi_out = wi;
+    *f_out = f;
     *pdf_out = p;
     return true;
 }
@@ -264,13 +315,15 @@ __device__ __forceinline__ float env_pdf_uv(const DevEnv& E, f2 uv) {
     uint32_t col = min(sat_usize(uv.x * (float)E.width), E.width - 1);
     return __ldg(E.cond_pdf + (size_t)row * E.width + col) * __ldg(E.marg_pdf + row);
 }
-__device__ __forceinline__ float env_pdf(const DevEnv& E, f3 wi) {  // light.rs:340-349
-    f2 uv = env_dir_to_uv(wi);
+// HdriEnvironmentLight::pdf (light.rs:340-349) at the texture coordinates of
+// the direction.
+__device__ __forceinline__ float env_pdf_at(const DevEnv& E, f2 uv) {
     float theta = uv.y * PYRE_PI;
     float st = sinf(theta);
     if (st < 1e-6f) return 0.0f;
     return env_pdf_uv(E, uv) / (2.0f * PYRE_PI * PYRE_PI * st);
 }
+__device__ __forceinline__ float env_pdf(const DevEnv& E, f3 wi) { return env_pdf_at(E, env_dir_to_uv(wi)); }
 
 // Distribution1D::sample_continuous (distribution.rs:79-101) over a CDF row.
 __device__ __forceinline__ float cdf_sample(const float* cdf, uint32_t n, float u, float* pdf, uint32_t* bin_out) {

@@ -97,6 +97,10 @@ def test_disney_consistency_on_device(gpu_ctx, oracle_mod):
         # material.rs:332-387: the sample's f and pdf are eval and pdf of the sampled direction
         assert np.linalg.norm(fe - f, axis=1).max() < kat["tol"]
         assert np.abs(pe - pdf).max() < kat["tol"]
+        # the sample's f and pdf come from the fused evaluation shade uses;
+        # it must equal the separate eval and pdf to the bit
+        assert np.array_equal(f.view(np.uint32), fe.view(np.uint32))
+        assert np.array_equal(pdf.view(np.uint32), pe.view(np.uint32))
         assert pdf.min() > 0.0 and wi[:, 2].min() > 0.0
         # and the device agrees with the oracle draw by draw: the same sampled
         # directions (to the ulps of CUDA's and glibc's sin/cos), and the same
