@@ -244,6 +244,34 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
     }
 }
 
+// Depth-0 order of a single view's wave: extend and shade take the camera
+// paths in 8x4 pixel tiles, so a warp's 32 rays cover a compact footprint
+// instead of 32 pixels of one row. j -> path index k * npix + p is a
+// bijection of [0, k_valid * npix): tiles run along bands of 4 crop rows (the
+// last band may be shorter), and a band's last cw % 8 columns are taken row by
+// row. Path indices, seeds and the film's sample order stay row-major.
+#define PYRE_TILE_W 8u
+#define PYRE_TILE_H 4u
+__device__ __forceinline__ uint32_t tiled_path(const WaveParams& W, uint32_t j) {
+    const uint32_t k = j / W.npix, q = j - k * W.npix;
+    const uint32_t band_px = W.cw * PYRE_TILE_H, full_bands = W.ch / PYRE_TILE_H;
+    uint32_t band = q / band_px, hb = PYRE_TILE_H;
+    if (band >= full_bands) { band = full_bands; hb = W.ch - full_bands * PYRE_TILE_H; }
+    const uint32_t r = q - band * band_px;
+    const uint32_t cwt = W.cw - W.cw % PYRE_TILE_W;  // columns in whole tiles
+    uint32_t x, y;
+    if (r < hb * cwt) {
+        const uint32_t tile_px = PYRE_TILE_W * hb, c = r / tile_px, l = r - c * tile_px;
+        x = c * PYRE_TILE_W + l % PYRE_TILE_W;
+        y = l / PYRE_TILE_W;
+    } else {
+        const uint32_t rw = W.cw - cwt, rem = r - hb * cwt;
+        x = cwt + rem % rw;
+        y = rem / rw;
+    }
+    return k * W.npix + (band * PYRE_TILE_H + y) * W.cw + x;
+}
+
 // ---------------------------------------------------------------- extend --
 // Path state is read and written once per stage through the live-path
 // queues, so the traversal and shade kernels access it with streaming cache
@@ -255,9 +283,9 @@ struct ExtendRays {
     const DevScene* S;
     const PathSoA* P;
     const WaveParams* W;
-    const uint32_t* qin;  // live-path queue; null at depth 0 (path j)
+    const uint32_t* qin;  // live-path queue; null at depth 0 (every path of the wave)
     __device__ __forceinline__ uint32_t load(uint32_t j, TraceRay& r, int32_t& root) const {
-        const uint32_t i = qin ? __ldcs(qin + j) : j;
+        const uint32_t i = qin ? __ldcs(qin + j) : (BATCH ? j : tiled_path(*W, j));
         const float4 ro = __ldcs(P->ray_o + i), rd = __ldcs(P->ray_d + i);
         r.o = mk3(ro.x, ro.y, ro.z);
         r.d = mk3(rd.x, rd.y, rd.z);
@@ -443,7 +471,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
     const bool last_was_specular = depth == 0;  // no specular BSDFs: only camera rays
     const float INF = __int_as_float(0x7f800000);
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t i = W.sort ? P.qsort[j] : (depth == 0 ? j : __ldcs(qin + j));
+        const uint32_t i = W.sort ? P.qsort[j] : (depth > 0 ? __ldcs(qin + j) : (BATCH ? j : tiled_path(W, j)));
         float4 Lq = __ldcs(P.L + i);
         f3 L = mk3(Lq.x, Lq.y, Lq.z);
         f3 delta = splat3(0.0f), Ltot = splat3(0.0f);
