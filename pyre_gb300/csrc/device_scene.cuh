@@ -97,6 +97,10 @@ struct TraceHit {
 };
 
 #define PYRE_STACK 64
+// lanes of a warp that may still be looking for a leaf when the leaf phase starts
+#ifndef PYRE_LEAF_WAIT
+#define PYRE_LEAF_WAIT 12
+#endif
 
 // Rust-order slab test (bvh.rs:146-153): t1/t2 per axis, max of mins vs
 // t_min, min of maxes vs t_max, hit iff tmin <= tmax. Returns the entry.
@@ -159,12 +163,13 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 // With WIDTH 4 or 8 the instance BVHs are wide: a node step tests every
 // child box, continues with the nearest hit child and pushes the others
 // farthest first; leaf children are parked when they are reached.
-// Inner nodes are stepped while any lane of the warp still needs a leaf; a
-// lane that already holds one leaf keeps stepping speculatively. Leaves found
-// on the way are parked (at most three triangle ranges, all of the current
-// instance: a lane holding leaves does not leave or enter an instance) and
-// then tested by all lanes in lock step. An any-hit lane that finds a hit is
-// finished at the end of that leaf phase.
+// Inner nodes are stepped while more than PYRE_LEAF_WAIT lanes of the warp
+// still need a leaf (or no lane holds one); a lane that already holds one
+// leaf keeps stepping speculatively. Leaves found on the way are parked (at
+// most three triangle ranges, all of the current instance: a lane holding
+// leaves does not leave or enter an instance) and then tested by all lanes in
+// lock step. An any-hit lane that finds a hit is finished at the end of that
+// leaf phase.
 //
 // Src supplies the rays and takes the results:
 //   uint32_t load(uint32_t j, TraceRay& r, int32_t& root)  ray j of the queue,
@@ -276,8 +281,15 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
             if (drained) break;
             continue;
         }
-        // ---- inner phase: step nodes until every lane holds a leaf or has none left
-        while (__any_sync(FULL, active && !exhausted && !hit_any && parked == 0)) {
+        // ---- inner phase: step nodes until at most PYRE_LEAF_WAIT lanes still
+        // look for a leaf. Those lanes sit out the leaf phase and resume after
+        // it; the others do not idle until the slowest lane reaches its first
+        // leaf. The phase also runs while no lane holds a leaf to test, so each
+        // round makes progress.
+        while (true) {
+            const int seeking = __popc(__ballot_sync(FULL, active && !exhausted && !hit_any && parked == 0));
+            if (seeking == 0) break;
+            if (seeking <= PYRE_LEAF_WAIT && __any_sync(FULL, active && !hit_any && parked > 0)) break;
             if (!active || exhausted || hit_any || parked >= STOP) continue;
             if (node == PYRE_NODE_NONE) {
                 if (sp == 0) { exhausted = true; continue; }
