@@ -157,19 +157,44 @@ __device__ __forceinline__ void env_texel_weights(const DevEnv& E, f2 uv, uint32
     idx[3] = (uint32_t)(y1 * w + x1); wt[3] = dx * dy;
 }
 
+// Warp aggregation of the gradient atomics. The lanes of a warp (those
+// converged here) that add to the same address first sum their terms, and
+// one lane adds the sum. Many paths share a material, and importance
+// sampling sends most environment samples to the few texels of a bright
+// lobe, so one atomic per term serializes on those addresses.
+//
+// peer_sum: the sum of v over the lanes in `peers`; every lane of `peers`
+// calls it with the same mask. The leader's value is the one used.
+template <class T>
+__device__ __forceinline__ T peer_sum(unsigned peers, T v) {
+    if (peers == 0xffffffffu) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        return v;
+    }
+    T s = T(0);
+    for (unsigned rest = peers; rest; rest &= rest - 1) s += __shfl_sync(peers, v, __ffs(rest) - 1);
+    return s;
+}
+
 // d(loss)/d(texel) for a radiance term c * Le(uv), Le = texture(uv) * intensity.
 __device__ __forceinline__ void scatter_env(const DevEnv& E, float* env_grad, f2 uv, f3 c) {
     if (!env_grad) return;
     uint32_t idx[4];
     float wt[4];
     env_texel_weights(E, uv, idx, wt);
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const float s = wt[k] * E.intensity;
-        if (s == 0.0f) continue;
-        atomicAdd(env_grad + 3 * (size_t)idx[k], c.x * s);
-        atomicAdd(env_grad + 3 * (size_t)idx[k] + 1, c.y * s);
-        atomicAdd(env_grad + 3 * (size_t)idx[k] + 2, c.z * s);
+        const uint32_t key = s != 0.0f ? idx[k] : 0xffffffffu;  // zero weights add nothing
+        const unsigned peers = __match_any_sync(act, key);
+        const float x = peer_sum(peers, c.x * s), y = peer_sum(peers, c.y * s), z = peer_sum(peers, c.z * s);
+        if (key == 0xffffffffu || lane != __ffs(peers) - 1) continue;
+        atomicAdd(env_grad + 3 * (size_t)key, x);
+        atomicAdd(env_grad + 3 * (size_t)key + 1, y);
+        atomicAdd(env_grad + 3 * (size_t)key + 2, z);
     }
 }
 

@@ -349,14 +349,18 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene S, PathSoA P, WavePa
 }
 
 // ------------------------------------------------------- adjoint helpers --
-// Adds d loss / d (6 parameters of material m), summed per block in shared
-// memory when it fits, else straight into the FP64 gradient.
+// Adds d loss / d (6 parameters of material m): summed in FP64 over the
+// converged lanes of the warp with the same material (peer_sum), then per
+// block in shared memory when it fits, else straight into the FP64 gradient.
 __device__ __forceinline__ void add_material_grad(const WaveParams& W, double* sgrad, uint32_t m, const float g[6]) {
+    const unsigned peers = __match_any_sync(__activemask(), m);
+    const bool leader = (int)(threadIdx.x & 31) == __ffs(peers) - 1;
 #pragma unroll
     for (int k = 0; k < PYRE_NPARAM; ++k) {
-        if (g[k] == 0.0f) continue;
-        if (W.smem_grad) atomicAdd(sgrad + PYRE_NPARAM * m + k, (double)g[k]);
-        else atomicAdd(W.mat_grad + PYRE_NPARAM * (size_t)m + k, (double)g[k]);
+        const double v = peer_sum(peers, (double)g[k]);
+        if (!leader || v == 0.0) continue;
+        if (W.smem_grad) atomicAdd(sgrad + PYRE_NPARAM * m + k, v);
+        else atomicAdd(W.mat_grad + PYRE_NPARAM * (size_t)m + k, v);
     }
 }
 // d loss . (J (x) w): the parameter gradient of a term  w (x) f(wo, wi).
