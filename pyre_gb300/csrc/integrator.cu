@@ -565,12 +565,10 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
             f3 o_local = moved ? ray_o - off : ray_o;
             f3 p = o_local + ray_d * t;
             if (moved) p = p + off;
-            const float4 A = __ldg(S.tris + 3 * (size_t)slot);
+            const uint4 vx = __ldg(S.slot_index + slot);  // does not wait for the instance
             f3 ns;
             if (I.normal_base >= 0) {
-                const uint32_t tri = __float_as_uint(A.w);
-                const uint32_t* ix = S.index + I.index_base + 3 * (size_t)tri;
-                const uint32_t a = ix[0], b = ix[1], c = ix[2];
+                const uint32_t a = vx.x, b = vx.y, c = vx.z;
                 const f3 na = mk3(S.normal[3 * (size_t)a], S.normal[3 * (size_t)a + 1], S.normal[3 * (size_t)a + 2]);
                 const f3 nb = mk3(S.normal[3 * (size_t)b], S.normal[3 * (size_t)b + 1], S.normal[3 * (size_t)b + 2]);
                 const f3 nc = mk3(S.normal[3 * (size_t)c], S.normal[3 * (size_t)c + 1], S.normal[3 * (size_t)c + 2]);
