@@ -207,7 +207,7 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
     const uint32_t n = P.ctl->n_valid;
     const uint32_t s_base = P.ctl->s_base;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t x, y, s, width, height;
+        uint32_t x, y, s, width, height, max_depth = W.max_depth;
         const DevCamera* cam = &W.cam;
         if (BATCH) {
             const DevWave& wv = W.waves[P.ctl->wave];
@@ -216,6 +216,7 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
             const uint32_t local = i - sg.path_base, k = local / J.npix, p = local - k * J.npix;
             x = p % J.width; y = p / J.width; s = sg.s_first + k;
             width = J.width; height = J.height;
+            max_depth = J.max_depth;
             cam = &J.cam;
             P.pjob[i] = sg.job;
         } else {
@@ -236,10 +237,13 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
         P.ray_o[i] = make_float4(o.x, o.y, o.z, 1e-4f);
         P.ray_d[i] = make_float4(d.x, d.y, d.z, time);
         store_rng(P.rng, i, g);
-        P.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-        P.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        P.aov_a[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        P.aov_n[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        // radiance 0, throughput 1 and the AOVs are set by shade at depth 0;
+        // with max_depth 0 no vertex is shaded and the sample is all zeros
+        if (max_depth == 0) {
+            P.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            P.aov_a[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            P.aov_n[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
         for (uint32_t s = 0; s < W.ns; ++s) P.pend[(size_t)i * W.ns + s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 }
@@ -476,7 +480,10 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
     const float INF = __int_as_float(0x7f800000);
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         const uint32_t i = W.sort ? P.qsort[j] : (depth > 0 ? __ldcs(qin + j) : (BATCH ? j : tiled_path(W, j)));
-        float4 Lq = __ldcs(P.L + i);
+        // a batch wave traces every job's camera rays; a job with max_depth 0 shades none
+        if (BATCH && depth == 0 && W.jobs[P.pjob[i]].max_depth == 0) continue;
+        // a camera path starts with radiance 0 and throughput 1 (integrator.rs:63-64)
+        const float4 Lq = depth > 0 ? __ldcs(P.L + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         f3 L = mk3(Lq.x, Lq.y, Lq.z);
         f3 delta = splat3(0.0f), Ltot = splat3(0.0f);
         if (ADJ) {  // adjoint of this path's film pixel, and its forward radiance
@@ -512,7 +519,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
                 }
             }
         }
-        const float4 bq = __ldcs(P.beta + i);
+        const float4 bq = depth > 0 ? __ldcs(P.beta + i) : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         f3 beta = mk3(bq.x, bq.y, bq.z);
         const float last_pdf = bq.w;
         const float4 ro = __ldcs(P.ray_o + i), rd = __ldcs(P.ray_d + i);
@@ -523,6 +530,10 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
         bool alive = false;
 
         if (code == -1) {
+            if (depth == 0) {  // a camera ray that escapes leaves the AOVs at zero
+                P.aov_a[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                P.aov_n[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
             // Escaped: environment radiance with MIS against the BSDF arm (integrator.rs:243-259).
             if (S.has_env) {
                 const f2 uv = env_dir_to_uv(ray_d);

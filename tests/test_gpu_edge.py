@@ -25,6 +25,27 @@ def test_shallow_depths(gpu_ctx, oracle_mod, max_depth):
     np.testing.assert_allclose(film.depth, ref["depth"], rtol=1e-3, atol=1e-3)
 
 
+def test_zero_depth_is_all_zeros(gpu_ctx):
+    """max_depth 0 runs no bounce (integrator.rs:75): every channel of every
+    sample is zero, also for a job of that depth inside a batch."""
+    sc, cam = P.studio_ref(), P.studio_ref_camera(40, 24)
+    ds = gpu_ctx.upload(sc)
+    film = gpu_ctx.render(ds, cam, PathIntegrator(0, 3), 40, 24, 4)
+    for ch in (film.radiance, film.albedo, film.normal, film.depth):
+        assert not np.any(ch)
+    ds.close()
+    jobs = P.batch_jobs(n_jobs=3, seed=9, resolutions=(32,), spps=(2,), tri_range=(10, 500))
+    jobs[1]["integrator"] = PathIntegrator(0, 3)
+    db = gpu_ctx.upload_batch([j["scene"] for j in jobs])
+    spec = [{"part": k, "camera": j["camera"], "width": j["width"], "height": j["height"], "spp": j["spp"],
+             "integrator": j["integrator"]} for k, j in enumerate(jobs)]
+    films = gpu_ctx.render_batch(db, spec)
+    for ch in (films[1].radiance, films[1].albedo, films[1].normal, films[1].depth):
+        assert not np.any(ch)
+    assert np.any(films[0].radiance) and np.any(films[2].radiance)
+    db.close()
+
+
 def test_environment_only_scene(gpu_ctx, oracle_mod):
     sc = Scene()
     sc.env = HdriEnvironmentLight.gradient((0.2, 0.35, 0.65), (0.95, 0.85, 0.7), 1.5)
