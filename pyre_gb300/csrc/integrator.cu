@@ -311,11 +311,13 @@ struct ExtendRays {
     }
 };
 
-// The traversal kernels ask for 8 resident blocks of 128 threads (at most 64
-// registers, a few bytes of spill): 2 % faster on the 1080p studio frame than
-// the 7 blocks the unconstrained 70-register build allows.
+// The traversal kernels ask for 9 resident blocks of 128 threads (at most 56
+// registers; k_shadow spills about 100 bytes). Warps wait mostly on node,
+// triangle and stack loads, so more of them per SM pay. On the 1080p studio
+// frame 9 blocks beat 8 (64 registers) by 2 %, and 8 beat the 7 of the
+// unconstrained 70-register build by 2 %; 10 blocks (48 registers) lose 2 %.
 template <bool BATCH, int WIDTH>
-__global__ void __launch_bounds__(128, 8) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+__global__ void __launch_bounds__(128, 9) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1]};
     trace_stream<false, WIDTH>(S, src, P.ctl->count[depth], &P.ctl->fetch[2 * depth], W.refill);
 }
@@ -347,7 +349,7 @@ struct ShadowRays {
 };
 
 template <bool BATCH, int WIDTH>
-__global__ void __launch_bounds__(128, 8) k_shadow(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+__global__ void __launch_bounds__(128, 9) k_shadow(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ShadowRays<BATCH> src{&S, &P, &W};
     trace_stream<true, WIDTH>(S, src, P.ctl->scount[depth], &P.ctl->fetch[2 * depth + 1], W.refill);
 }
@@ -864,7 +866,7 @@ struct QueryRays {
 };
 
 template <bool ANY, int WIDTH>
-__global__ void __launch_bounds__(128) k_intersect(DevScene S, QueryRays q, uint32_t n, unsigned int* counter,
+__global__ void __launch_bounds__(128, 9) k_intersect(DevScene S, QueryRays q, uint32_t n, unsigned int* counter,
                                                    int refill) {
     QueryRays src = q;
     src.S = &S;
