@@ -233,8 +233,24 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
     bool exhausted = true;   // no node left to step
     // an 8-wide step can push 7 entries, so the 8-wide stack is deeper
     constexpr int STACK = WIDTH == 8 ? 96 : PYRE_STACK;
-    int stack[STACK];
+    // Any-hit traversal keeps the bottom 8 stack entries of each lane in
+    // shared memory (entry-major, so a lane always uses its own bank), the
+    // rest in local memory: the shadow stage is 4 % faster on the 1080p frame.
+    // Closest hit keeps the whole stack in local memory; with the same short
+    // stack it was 2 % slower (8 entries) and 4 % slower (16 entries).
+    constexpr int SK = ANY ? 8 : 0;
+    __shared__ int sstack[SK > 0 ? SK : 1][128];  // traversal blocks have at most 128 threads
+    int stack[STACK - SK];
     int sp = 0;
+    auto spush = [&](int v) {
+        if (SK > 0 && sp < SK) sstack[sp][threadIdx.x] = v;
+        else stack[sp - SK] = v;
+        ++sp;
+    };
+    auto spop = [&]() -> int {
+        --sp;
+        return (SK > 0 && sp < SK) ? sstack[sp][threadIdx.x] : stack[sp - SK];
+    };
     int node = PYRE_NODE_NONE;
     int inst = -1;
     int32_t inst_orig = 0;
@@ -295,17 +311,17 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
             if (!active || exhausted || hit_any || parked >= STOP) continue;
             if (node == PYRE_NODE_NONE) {
                 if (sp == 0) { exhausted = true; continue; }
-                node = stack[--sp];
+                node = spop();
             }
             if (node == PYRE_NODE_EXIT) {
-                if (parked) { stack[sp++] = PYRE_NODE_EXIT; node = PYRE_NODE_NONE; parked = STOP; continue; }
+                if (parked) { spush(PYRE_NODE_EXIT); node = PYRE_NODE_NONE; parked = STOP; continue; }
                 inst = -1;
                 o = r.o;
                 node = PYRE_NODE_NONE;
                 continue;
             }
             if (node & PYRE_TAG_INST) {
-                if (parked) { stack[sp++] = node; node = PYRE_NODE_NONE; parked = STOP; continue; }
+                if (parked) { spush(node); node = PYRE_NODE_NONE; parked = STOP; continue; }
                 const int k = node & ~PYRE_TAG_INST;
                 node = PYRE_NODE_NONE;
                 const DevInstance& I = S.inst[k];
@@ -319,7 +335,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                 float e;
                 if (!slab(I.lo[0], I.hi[0], I.lo[1], I.hi[1], I.lo[2], I.hi[2], lo, inv, r.tmin, best_t, &e)) continue;
                 if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
-                stack[sp++] = PYRE_NODE_EXIT;
+                spush(PYRE_NODE_EXIT);
                 inst = k;
                 inst_orig = I.orig_id;
                 o = lo;
@@ -369,7 +385,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                 if (sp + nh > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
 #pragma unroll
                 for (int k = WIDTH - 1; k >= 1; --k)
-                    if (ent[k] != PYRE_NODE_NONE) stack[sp++] = ent[k];
+                    if (ent[k] != PYRE_NODE_NONE) spush(ent[k]);
                 node = ent[0];
                 continue;
             }
@@ -386,9 +402,9 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                 const int need = (h0 && leaf0 ? nd.z : 0) + (h1 && leaf1 ? nd.w : 0) + 1;
                 if (sp + need > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                 if (h1 && leaf1)
-                    for (int k = nd.w - 1; k >= 0; --k) stack[sp++] = PYRE_TAG_INST | (nd.y + k);
+                    for (int k = nd.w - 1; k >= 0; --k) spush(PYRE_TAG_INST | (nd.y + k));
                 if (h0 && leaf0)
-                    for (int k = nd.z - 1; k >= 0; --k) stack[sp++] = PYRE_TAG_INST | (nd.x + k);
+                    for (int k = nd.z - 1; k >= 0; --k) spush(PYRE_TAG_INST | (nd.x + k));
             } else {
                 if (h0 && leaf0) { ls[parked] = nd.x; lc[parked] = nd.z; ++parked; }
                 if (h1 && leaf1) { ls[parked] = nd.y; lc[parked] = nd.w; ++parked; }
@@ -398,7 +414,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
             if (g0 && g1) {
                 const bool first0 = e0 <= e1;
                 if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
-                stack[sp++] = (first0 ? nd.y : nd.x) | tag;
+                spush((first0 ? nd.y : nd.x) | tag);
                 node = (first0 ? nd.x : nd.y) | tag;
             } else if (g0) {
                 node = nd.x | tag;
