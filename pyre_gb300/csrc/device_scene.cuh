@@ -99,10 +99,10 @@ struct TraceHit {
 };
 
 #define PYRE_STACK 64
-// lanes of a warp that may still be looking for a leaf when the leaf phase starts
-#ifndef PYRE_LEAF_WAIT
-#define PYRE_LEAF_WAIT 12
-#endif
+// lanes of a warp that may still be looking for a leaf when the leaf phase
+// starts, for closest-hit and any-hit traversal
+#define PYRE_LEAF_WAIT_CLOSEST 8
+#define PYRE_LEAF_WAIT_ANY 12
 
 // Rust-order slab test (bvh.rs:146-153): t1/t2 per axis, max of mins vs
 // t_min, min of maxes vs t_max, hit iff tmin <= tmax. Returns the entry.
@@ -165,7 +165,8 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 // With WIDTH 4 or 8 the instance BVHs are wide: a node step tests every
 // child box, continues with the nearest hit child and pushes the others
 // farthest first; leaf children are parked when they are reached.
-// Inner nodes are stepped while more than PYRE_LEAF_WAIT lanes of the warp
+// Inner nodes are stepped while more than 8 (closest hit) or 12 (any hit)
+// lanes of the warp
 // still need a leaf (or no lane holds one); a lane that already holds one
 // leaf keeps stepping speculatively. Leaves found on the way are parked (at
 // most three triangle ranges, all of the current instance: a lane holding
@@ -214,6 +215,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
     // a lane stops stepping nodes once it holds STOP parked leaves (a binary
     // step can park two, a wide step at most one)
     constexpr int STOP = WIDTH > 2 ? 3 : 2;
+    constexpr int LEAF_WAIT = ANY ? PYRE_LEAF_WAIT_ANY : PYRE_LEAF_WAIT_CLOSEST;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lanes_below = (1u << lane) - 1u;
@@ -299,7 +301,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
             if (drained) break;
             continue;
         }
-        // ---- inner phase: step nodes until at most PYRE_LEAF_WAIT lanes still
+        // ---- inner phase: step nodes until at most LEAF_WAIT lanes still
         // look for a leaf. Those lanes sit out the leaf phase and resume after
         // it; the others do not idle until the slowest lane reaches its first
         // leaf. The phase also runs while no lane holds a leaf to test, so each
@@ -307,7 +309,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
         while (true) {
             const int seeking = __popc(__ballot_sync(FULL, active && !exhausted && !hit_any && parked == 0));
             if (seeking == 0) break;
-            if (seeking <= PYRE_LEAF_WAIT && __any_sync(FULL, active && !hit_any && parked > 0)) break;
+            if (seeking <= LEAF_WAIT && __any_sync(FULL, active && !hit_any && parked > 0)) break;
             if (!active || exhausted || hit_any || parked >= STOP) continue;
             if (node == PYRE_NODE_NONE) {
                 if (sp == 0) { exhausted = true; continue; }

@@ -88,7 +88,8 @@ struct WaveParams {
     float* env_grad;     // env texels*3 or null
     uint32_t n_mat;
     int smem_grad;       // material gradients summed per block in shared memory
-    int refill;          // traversal: idle lanes of a warp that trigger a refetch
+    int refill;          // traversal: idle lanes of a warp that trigger a refetch (closest hit)
+    int refill_any;      // the same for the any-hit (shadow) traversal
     int sort;            // shade reads the live paths sorted by material (P.qsort)
     int bvh_width;       // instance BVH width of the traversal kernels: 2, 4 or 8
     // progressive accumulation (pyre_render_progressive): crop npix x 3 running
@@ -96,10 +97,14 @@ struct WaveParams {
     float* prog_mean;
 };
 
+// Default ray-refill thresholds (idle lanes of a warp) of closest-hit and
+// any-hit traversal; a nonzero refill_lanes sets both.
 #define PYRE_DEFAULT_REFILL 16
-static inline int refill_lanes(const pyre_render_params* rp) {
+#define PYRE_DEFAULT_REFILL_ANY 8
+static inline int refill_lanes(const pyre_render_params* rp, bool any_hit = false) {
     const uint32_t v = rp ? rp->refill_lanes : 0u;
-    return v == 0 ? PYRE_DEFAULT_REFILL : (int)std::min<uint32_t>(v, 32u);
+    if (v == 0) return any_hit ? PYRE_DEFAULT_REFILL_ANY : PYRE_DEFAULT_REFILL;
+    return (int)std::min<uint32_t>(v, 32u);
 }
 
 #define PYRE_GSLOT 4  // float4s of parked gradient terms per NEE slot
@@ -351,7 +356,7 @@ struct ShadowRays {
 template <bool BATCH, int WIDTH>
 __global__ void __launch_bounds__(128, 9) k_shadow(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ShadowRays<BATCH> src{&S, &P, &W};
-    trace_stream<true, WIDTH>(S, src, P.ctl->scount[depth], &P.ctl->fetch[2 * depth + 1], W.refill);
+    trace_stream<true, WIDTH>(S, src, P.ctl->scount[depth], &P.ctl->fetch[2 * depth + 1], W.refill_any);
 }
 
 // ------------------------------------------------------- adjoint helpers --
@@ -1144,6 +1149,7 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
     W.refill = refill_lanes(&rp);
+    W.refill_any = refill_lanes(&rp, true);
     W.sort = rp.sort_by_material ? 1 : 0;
     W.prog_mean = prog;
     DevScene D;
@@ -1326,6 +1332,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     W.max_depth = max_depth;
     W.ns = scene->part_light_max;
     W.refill = refill_lanes(params);
+    W.refill_any = refill_lanes(params, true);
     W.sort = params && params->sort_by_material ? 1 : 0;
     DevScene D;
     int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), params ? params->bvh_width : 0u, &D, &W.bvh_width);
@@ -1475,6 +1482,7 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
     W.refill = refill_lanes(&rp);
+    W.refill_any = refill_lanes(&rp, true);
     W.sort = rp.sort_by_material ? 1 : 0;
     DevScene D;
     int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width, false);
@@ -1542,15 +1550,13 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
 template <bool ANY>
 static void launch_intersect(pyre_ctx* ctx, const DevScene& D, const QueryRays& q, uint32_t n, int width) {
     cudaStream_t st = ctx->stream;
+    const int refill = ANY ? PYRE_DEFAULT_REFILL_ANY : PYRE_DEFAULT_REFILL;
     if (width == 8) {
-        k_intersect<ANY, 8><<<grid_for(ctx, k_intersect<ANY, 8>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter,
-                                                                                     PYRE_DEFAULT_REFILL);
+        k_intersect<ANY, 8><<<grid_for(ctx, k_intersect<ANY, 8>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter, refill);
     } else if (width == 4) {
-        k_intersect<ANY, 4><<<grid_for(ctx, k_intersect<ANY, 4>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter,
-                                                                                     PYRE_DEFAULT_REFILL);
+        k_intersect<ANY, 4><<<grid_for(ctx, k_intersect<ANY, 4>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter, refill);
     } else {
-        k_intersect<ANY, 2><<<grid_for(ctx, k_intersect<ANY, 2>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter,
-                                                                                     PYRE_DEFAULT_REFILL);
+        k_intersect<ANY, 2><<<grid_for(ctx, k_intersect<ANY, 2>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter, refill);
     }
 }
 
@@ -1724,6 +1730,7 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
     W.refill = refill_lanes(&rp);
+    W.refill_any = refill_lanes(&rp, true);
     W.sort = rp.sort_by_material ? 1 : 0;
     DevScene D;
     if ((rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width))) return rc;
