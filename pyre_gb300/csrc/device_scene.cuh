@@ -228,8 +228,6 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
     hit.inst = -1; hit.tri = -1; hit.light = -1; hit.t = 0.0f; hit.u = 0.0f; hit.v = 0.0f;
     f3 inv = splat3(0.0f);
     float best_t = 0.0f;
-    uint32_t best_key = 0xffffffffu;
-    int32_t best_orig = 0x7fffffff;
     bool found = false;
     bool hit_any = false;    // any-hit: the ray is occluded
     bool exhausted = true;   // no node left to step
@@ -255,7 +253,6 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
     };
     int node = PYRE_NODE_NONE;
     int inst = -1;
-    int32_t inst_orig = 0;
     f3 o = r.o;
     // up to three parked triangle ranges; a lane keeps stepping (speculatively)
     // while it holds at most one, so one node step never needs more than three
@@ -279,18 +276,15 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                     id = src.load(j, r, root);
                     active = true;
                     inv = mk3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
-                    hit.inst = -1; hit.tri = -1; hit.light = -1;
-                    hit.t = r.tmax; hit.u = 0.0f; hit.v = 0.0f;
+                    hit.inst = -1; hit.tri = -1;
+                    hit.u = 0.0f; hit.v = 0.0f;
                     best_t = r.tmax;
-                    best_key = 0xffffffffu;
-                    best_orig = 0x7fffffff;
                     found = false;
                     hit_any = false;
                     exhausted = root < 0;
                     sp = 0;
                     node = exhausted ? PYRE_NODE_NONE : (root | PYRE_TAG_TOP);
                     inst = -1;
-                    inst_orig = 0;
                     o = r.o;
                     parked = 0;
                     lc[0] = lc[1] = lc[2] = 0;
@@ -339,7 +333,6 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                 if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                 spush(PYRE_NODE_EXIT);
                 inst = k;
-                inst_orig = I.orig_id;
                 o = lo;
                 node = root;
                 continue;
@@ -438,23 +431,28 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
             if (!mt_test(o, r.d, A, B, C, &t, &u, &v)) continue;
             if (!(t > r.tmin && t < r.tmax)) continue;
             if (ANY) { found = true; hit_any = true; continue; }
-            const uint32_t key = __float_as_uint(A.w);
             bool better = t < best_t;
-            if (!better && t == best_t && found)
-                better = inst_orig < best_orig || (inst_orig == best_orig && key < best_key);
+            if (!better && t == best_t && found) {
+                // a tie (rare): the lower Scene::primitives index, then the lower
+                // triangle id, wins; both are read back from the records
+                const int32_t cur = S.inst[inst].orig_id, best = S.inst[hit.inst].orig_id;
+                const uint32_t key = __float_as_uint(A.w);
+                const uint32_t best_key = __float_as_uint(__ldg(S.tris + 3 * (size_t)hit.tri).w);
+                better = cur < best || (cur == best && key < best_key);
+            }
             if (better) {
                 best_t = t;
                 found = true;
-                hit.t = t; hit.u = u; hit.v = v;
+                hit.u = u; hit.v = v;
                 hit.inst = inst; hit.tri = slot;
-                best_key = key;
-                best_orig = inst_orig;
             }
         }
         parked = 0;
         lc[0] = lc[1] = lc[2] = 0;
         // ---- finished rays hand over their result; the lane becomes idle
         if (active && (exhausted || hit_any)) {
+            hit.t = best_t;
+            hit.light = -1;
             src.store(id, r, hit, found);
             active = false;
         }
