@@ -167,6 +167,7 @@ __device__ __forceinline__ void env_texel_weights(const DevEnv& E, f2 uv, uint32
 // calls it with the same mask. The leader's value is the one used.
 template <class T>
 __device__ __forceinline__ T peer_sum(unsigned peers, T v) {
+    if ((peers & (peers - 1u)) == 0u) return v;  // alone
     if (peers == 0xffffffffu) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -175,6 +176,14 @@ __device__ __forceinline__ T peer_sum(unsigned peers, T v) {
     T s = T(0);
     for (unsigned rest = peers; rest; rest &= rest - 1) s += __shfl_sync(peers, v, __ffs(rest) - 1);
     return s;
+}
+
+// Full-warp sum of v (all 32 lanes call it).
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
 // d(loss)/d(texel) for a radiance term c * Le(uv), Le = texture(uv) * intensity.
@@ -196,6 +205,105 @@ __device__ __forceinline__ void scatter_env(const DevEnv& E, float* env_grad, f2
         atomicAdd(env_grad + 3 * (size_t)key + 1, y);
         atomicAdd(env_grad + 3 * (size_t)key + 2, z);
     }
+}
+
+}  // namespace pyre
+
+namespace pyre {
+
+#define PYRE_NO_KEY 0xffffffffu
+#define PYRE_FLUSH_ROUNDS 3  // keys aggregated per flush; the rest add directly
+
+// One lane's gradient terms of one path vertex, added at a point where the
+// warp is converged (warp_flush): the 6 parameters of one material (all the
+// terms of a vertex belong to the material of the previous vertex), and one
+// environment footprint (c, added to the 4 texels of uv's bilinear lookup).
+struct GradTerms {
+    uint32_t mat = PYRE_NO_KEY;
+    float g[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    bool env = false;
+    f2 uv;
+    f3 c;
+};
+
+// Adds every lane's terms. With all 32 lanes converged, the lanes holding the
+// same material (or the same footprint) are summed with full-warp butterflies
+// (FP64 for materials), for up to PYRE_FLUSH_ROUNDS keys per kind that more
+// than one lane holds, and one lane adds each sum; every other lane adds its
+// own terms. A warp that is not converged adds lane by lane.
+__device__ __forceinline__ void warp_flush(const DevScene& S, float* env_grad, double* mat_grad, double* sgrad,
+                                           bool smem, const GradTerms& t) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool full = __activemask() == FULL;
+    auto mat_add = [&](uint32_t m, int k, double v) {
+        if (v == 0.0) return;
+        if (smem) atomicAdd(sgrad + PYRE_NPARAM * m + k, v);
+        else atomicAdd(mat_grad + PYRE_NPARAM * (size_t)m + k, v);
+    };
+    // materials
+    bool left = t.mat != PYRE_NO_KEY;
+    if (full) {
+        // only keys that several lanes hold are worth a butterfly
+        const unsigned peers = __match_any_sync(FULL, t.mat);
+        unsigned todo = __ballot_sync(FULL, left && (peers & (peers - 1u)) != 0u);
+        for (int r = 0; r < PYRE_FLUSH_ROUNDS && todo; ++r) {
+            const int src = __ffs(todo) - 1;
+            const uint32_t key = __shfl_sync(FULL, t.mat, src);
+            const bool mine = left && t.mat == key;
+            todo &= ~__ballot_sync(FULL, mine);
+#pragma unroll
+            for (int k = 0; k < PYRE_NPARAM; ++k) {
+                const double v = warp_sum(mine ? (double)t.g[k] : 0.0);
+                if (lane == src) mat_add(key, k, v);
+            }
+            if (mine) left = false;
+        }
+    }
+    if (left)
+        for (int k = 0; k < PYRE_NPARAM; ++k) mat_add(t.mat, k, (double)t.g[k]);
+    // environment footprint
+    if (!env_grad) return;
+    uint32_t idx[4];
+    float wt[4];
+    f3 c = splat3(0.0f);
+    uint32_t key = PYRE_NO_KEY;
+    if (t.env) {
+        env_texel_weights(S.env, t.uv, idx, wt);
+        key = idx[0];  // the other three texels follow from the first
+        c = t.c * S.env.intensity;
+    }
+    left = key != PYRE_NO_KEY;
+    if (full) {
+        const unsigned peers = __match_any_sync(FULL, key);
+        unsigned todo = __ballot_sync(FULL, left && (peers & (peers - 1u)) != 0u);
+        for (int r = 0; r < PYRE_FLUSH_ROUNDS && todo; ++r) {
+            const int src = __ffs(todo) - 1;
+            const uint32_t k0 = __shfl_sync(FULL, key, src);
+            const bool mine = left && key == k0;
+            todo &= ~__ballot_sync(FULL, mine);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float x = warp_sum(mine ? c.x * wt[q] : 0.0f), y = warp_sum(mine ? c.y * wt[q] : 0.0f),
+                            z = warp_sum(mine ? c.z * wt[q] : 0.0f);
+                if (lane == src) {
+                    const size_t a = 3 * (size_t)idx[q];
+                    if (x != 0.0f) atomicAdd(env_grad + a, x);
+                    if (y != 0.0f) atomicAdd(env_grad + a + 1, y);
+                    if (z != 0.0f) atomicAdd(env_grad + a + 2, z);
+                }
+            }
+            if (mine) left = false;
+        }
+    }
+    if (left)
+        for (int q = 0; q < 4; ++q) {
+            if (wt[q] == 0.0f) continue;
+            const size_t a = 3 * (size_t)idx[q];
+            atomicAdd(env_grad + a, c.x * wt[q]);
+            atomicAdd(env_grad + a + 1, c.y * wt[q]);
+            atomicAdd(env_grad + a + 2, c.z * wt[q]);
+        }
 }
 
 }  // namespace pyre

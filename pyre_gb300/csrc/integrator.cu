@@ -360,20 +360,6 @@ __global__ void __launch_bounds__(128, 9) k_shadow(DevScene S, PathSoA P, WavePa
 }
 
 // ------------------------------------------------------- adjoint helpers --
-// Adds d loss / d (6 parameters of material m): summed in FP64 over the
-// converged lanes of the warp with the same material (peer_sum), then per
-// block in shared memory when it fits, else straight into the FP64 gradient.
-__device__ __forceinline__ void add_material_grad(const WaveParams& W, double* sgrad, uint32_t m, const float g[6]) {
-    const unsigned peers = __match_any_sync(__activemask(), m);
-    const bool leader = (int)(threadIdx.x & 31) == __ffs(peers) - 1;
-#pragma unroll
-    for (int k = 0; k < PYRE_NPARAM; ++k) {
-        const double v = peer_sum(peers, (double)g[k]);
-        if (!leader || v == 0.0) continue;
-        if (W.smem_grad) atomicAdd(sgrad + PYRE_NPARAM * m + k, v);
-        else atomicAdd(W.mat_grad + PYRE_NPARAM * (size_t)m + k, v);
-    }
-}
 // d loss . (J (x) w): the parameter gradient of a term  w (x) f(wo, wi).
 __device__ __forceinline__ void jac_dot(const Bsdf& b, f3 wo, f3 wi, f3 w, float g[6]) {
     float J[3][PYRE_NPARAM];
@@ -381,20 +367,21 @@ __device__ __forceinline__ void jac_dot(const Bsdf& b, f3 wo, f3 wi, f3 w, float
 #pragma unroll
     for (int k = 0; k < PYRE_NPARAM; ++k) g[k] = w.x * J[0][k] + w.y * J[1][k] + w.z * J[2][k];
 }
-// Applies the parked gradient terms of one visible NEE slot (layout:
+// Collects the parked gradient terms of one visible NEE slot (layout:
 // g0 = params 0-3, g1 = (params 4-5, material bits, pending), g2 = (env uv,
-// env flag, -), g3 = (env texel weight rgb, -)).
-__device__ __forceinline__ void apply_parked_grad(const DevScene& S, const WaveParams& W, double* sgrad,
-                                                  const float4* G) {
+// env flag, -), g3 = (env texel weight rgb, -)). All slots of a vertex share
+// its material, and at most one (the environment's) has a footprint.
+__device__ __forceinline__ void collect_parked_grad(const float4* G, GradTerms& t) {
     const float4 g0 = G[0], g1 = G[1];
     if (g1.w == 0.0f) return;
-    const float g[6] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y};
-    add_material_grad(W, sgrad, __float_as_uint(g1.z), g);
+    t.mat = __float_as_uint(g1.z);
+    t.g[0] += g0.x; t.g[1] += g0.y; t.g[2] += g0.z; t.g[3] += g0.w; t.g[4] += g1.x; t.g[5] += g1.y;
     const float4 g2 = G[2];
     if (g2.z != 0.0f) {
         const float4 g3 = G[3];
-        f2 uv; uv.x = g2.x; uv.y = g2.y;
-        scatter_env(S.env, W.env_grad, uv, mk3(g3.x, g3.y, g3.z));
+        t.env = true;
+        t.uv.x = g2.x; t.uv.y = g2.y;
+        t.c = mk3(g3.x, g3.y, g3.z);
     }
 }
 
@@ -500,13 +487,14 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
             Ltot = mk3(lt.x, lt.y, lt.z);
         }
         // Contributions left by the previous vertex's NEE, in light order.
+        GradTerms gt;  // ADJ: this vertex's terms for the previous vertex's material
         if (depth > 0) {
             for (uint32_t s = 0; s < W.ns; ++s) {
                 float4 c = P.pend[(size_t)i * W.ns + s];
                 if (c.w != 0.0f) {
                     L = L + mk3(c.x, c.y, c.z);
                     P.pend[(size_t)i * W.ns + s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if (ADJ) apply_parked_grad(S, W, sgrad, P.gpend + PYRE_GSLOT * ((size_t)i * W.ns + s));
+                    if (ADJ) collect_parked_grad(P.gpend + PYRE_GSLOT * ((size_t)i * W.ns + s), gt);
                 }
             }
             if (ADJ) {
@@ -521,11 +509,14 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
                         const uint32_t m = __float_as_uint(b0.w);
                         float g[6];
                         jac_dot(load_bsdf(S, m), mk3(b0.x, b0.y, b0.z), mk3(b1.x, b1.y, b1.z), w, g);
-                        add_material_grad(W, sgrad, m, g);
+                        gt.mat = m;
+#pragma unroll
+                        for (int k = 0; k < PYRE_NPARAM; ++k) gt.g[k] += g[k];
                     }
                 }
             }
         }
+        if (ADJ) warp_flush(S, W.env_grad, W.mat_grad, sgrad, W.smem_grad != 0, gt);
         const float4 bq = depth > 0 ? __ldcs(P.beta + i) : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         f3 beta = mk3(bq.x, bq.y, bq.z);
         const float last_pdf = bq.w;
@@ -727,10 +718,13 @@ __global__ void k_accumulate_adjoint(DevScene S, PathSoA P, WaveParams W) {
         __syncthreads();
     }
     const uint32_t n = P.ctl->n_valid;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        GradTerms gt;
         for (uint32_t s = 0; s < W.ns; ++s)
             if (P.pend[(size_t)i * W.ns + s].w != 0.0f)
-                apply_parked_grad(S, W, sgrad, P.gpend + PYRE_GSLOT * ((size_t)i * W.ns + s));
+                collect_parked_grad(P.gpend + PYRE_GSLOT * ((size_t)i * W.ns + s), gt);
+        warp_flush(S, W.env_grad, W.mat_grad, sgrad, W.smem_grad != 0, gt);
+    }
     if (W.smem_grad) {
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x)
