@@ -120,8 +120,8 @@ struct PathSoA {
     float4* aov_a;     // albedo.xyz, depth
     float4* aov_n;     // normal.xyz
     float4* pend;      // ns per path: NEE contribution.xyz, w = 1 while pending
-    float4* sh_o;      // ns per path: shadow origin.xyz, t_max
-    float4* sh_d;      // ns per path: shadow direction.xyz, time
+    float4* sh_o;      // per shadow-queue entry: shadow origin.xyz, t_max
+    float4* sh_d;      // per shadow-queue entry: shadow direction.xyz, time
     uint32_t* q[2];
     uint32_t* qsort;   // the live paths of the current depth ordered by shade_key
     uint32_t* sq;
@@ -336,8 +336,9 @@ struct ShadowRays {
     const PathSoA* P;
     const WaveParams* W;
     __device__ __forceinline__ uint32_t load(uint32_t j, TraceRay& r, int32_t& root) const {
+        // the ray sits at its queue entry, so these loads do not wait for sq
         const uint32_t target = __ldcs(P->sq + j);
-        const float4 so = __ldcs(P->sh_o + target), sd = __ldcs(P->sh_d + target);
+        const float4 so = __ldcs(P->sh_o + j), sd = __ldcs(P->sh_d + j);
         r.o = mk3(so.x, so.y, so.z);
         r.d = mk3(sd.x, sd.y, sd.z);
         r.tmin = 1e-3f;
@@ -691,9 +692,10 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
                         G[1] = make_float4(gm[4], gm[5], __uint_as_float(I.material), 1.0f);
                     }
                     if (sh_ray) {
-                        P.sh_o[sidx] = make_float4(p_off.x, p_off.y, p_off.z, sh_tmax);
-                        P.sh_d[sidx] = make_float4(sh_dir.x, sh_dir.y, sh_dir.z, time);
-                        P.sq[append_slot(shadow_count)] = (uint32_t)sidx;
+                        const uint32_t q = append_slot(shadow_count);
+                        P.sh_o[q] = make_float4(p_off.x, p_off.y, p_off.z, sh_tmax);
+                        P.sh_d[q] = make_float4(sh_dir.x, sh_dir.y, sh_dir.z, time);
+                        P.sq[q] = (uint32_t)sidx;
                     }
                 }
                 store_rng(P.rng, i, g);
