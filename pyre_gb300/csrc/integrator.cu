@@ -110,8 +110,11 @@ static inline int refill_lanes(const pyre_render_params* rp, bool any_hit = fals
 #define PYRE_GSLOT 4  // float4s of parked gradient terms per NEE slot
 
 struct PathSoA {
-    float4* ray_o;     // origin.xyz
-    float4* ray_d;     // direction.xyz, time
+    // rays and hits live at queue positions: entry j of the depth's live-path
+    // queue (at depth 0, the path index). Depth d reads ray_o/ray_d[d & 1];
+    // shade writes the next depth's rays into the other buffer.
+    float4* ray_o[2];  // origin.xyz
+    float4* ray_d[2];  // direction.xyz, time
     float4* hit;       // t, u, v, triangle slot (bits)
     int32_t* hit_inst; // instance slot; -1 miss; -2-l quad light l
     uint4* rng;        // 2 per path
@@ -239,8 +242,8 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
         float time = g.next_f32();
         f3 o, d;
         camera_ray(*cam, ndc, lens, &o, &d);
-        P.ray_o[i] = make_float4(o.x, o.y, o.z, 1e-4f);
-        P.ray_d[i] = make_float4(d.x, d.y, d.z, time);
+        P.ray_o[0][i] = make_float4(o.x, o.y, o.z, 1e-4f);
+        P.ray_d[0][i] = make_float4(d.x, d.y, d.z, time);
         store_rng(P.rng, i, g);
         // radiance 0, throughput 1 and the AOVs are set by shade at depth 0;
         // with max_depth 0 no vertex is shaded and the sample is all zeros
@@ -293,26 +296,28 @@ struct ExtendRays {
     const PathSoA* P;
     const WaveParams* W;
     const uint32_t* qin;  // live-path queue; null at depth 0 (every path of the wave)
+    uint32_t depth;
+    // ray j of the queue sits at queue position j (depth 0: path tiled_path(j))
     __device__ __forceinline__ uint32_t load(uint32_t j, TraceRay& r, int32_t& root) const {
-        const uint32_t i = qin ? __ldcs(qin + j) : (BATCH ? j : tiled_path(*W, j));
-        const float4 ro = __ldcs(P->ray_o + i), rd = __ldcs(P->ray_d + i);
+        const uint32_t p = qin ? j : (BATCH ? j : tiled_path(*W, j));
+        const float4 ro = __ldcs(P->ray_o[depth & 1] + p), rd = __ldcs(P->ray_d[depth & 1] + p);
         r.o = mk3(ro.x, ro.y, ro.z);
         r.d = mk3(rd.x, rd.y, rd.z);
         r.tmin = 1e-4f;
         r.tmax = __int_as_float(0x7f800000);
         r.time = rd.w;
-        root = BATCH ? W->jobs[P->pjob[i]].tlas_root : S->tlas_root;
-        return i;
+        root = BATCH ? W->jobs[P->pjob[qin ? __ldcs(qin + p) : p]].tlas_root : S->tlas_root;
+        return p;
     }
-    __device__ __forceinline__ void store(uint32_t i, const TraceRay& r, TraceHit& h, bool) const {
+    __device__ __forceinline__ void store(uint32_t p, const TraceRay& r, TraceHit& h, bool) const {
         uint32_t lfirst = 0, lcount = S->n_lights;
         if (BATCH) {
-            const DevJob& J = W->jobs[P->pjob[i]];
+            const DevJob& J = W->jobs[P->pjob[qin ? __ldcs(qin + p) : p]];
             lfirst = J.light_first; lcount = J.light_count;
         }
         hit_quad_lights(*S, r, lfirst, lcount, &h);
-        __stcs(P->hit + i, make_float4(h.t, h.u, h.v, __int_as_float(h.tri)));
-        __stcs(P->hit_inst + i, h.light >= 0 ? -2 - h.light : h.inst);
+        __stcs(P->hit + p, make_float4(h.t, h.u, h.v, __int_as_float(h.tri)));
+        __stcs(P->hit_inst + p, h.light >= 0 ? -2 - h.light : h.inst);
     }
 };
 
@@ -323,7 +328,7 @@ struct ExtendRays {
 // unconstrained 70-register build by 2 %; 10 blocks (48 registers) lose 2 %.
 template <bool BATCH, int WIDTH>
 __global__ void __launch_bounds__(128, 9) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
-    ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1]};
+    ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1], depth};
     trace_stream<false, WIDTH>(S, src, P.ctl->count[depth], &P.ctl->fetch[2 * depth], W.refill);
 }
 
@@ -400,11 +405,9 @@ __device__ __forceinline__ uint32_t shade_key(const DevScene& S, int32_t code) {
 
 __global__ void k_sort_count(DevScene S, PathSoA P, uint32_t depth) {
     const uint32_t n = P.ctl->count[depth];
-    const uint32_t* qin = P.q[depth & 1];
     const int lane = threadIdx.x & 31;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t i = depth == 0 ? j : qin[j];
-        const uint32_t key = shade_key(S, P.hit_inst[i]);
+        const uint32_t key = shade_key(S, P.hit_inst[j]);
         const unsigned peers = __match_any_sync(__activemask(), key);
         if (lane == __ffs(peers) - 1) atomicAdd(&P.ctl->sort_hist[key], (uint32_t)__popc(peers));
     }
@@ -440,18 +443,16 @@ __global__ void __launch_bounds__(PYRE_SORT_BINS) k_sort_scan(PathSoA P) {
 
 __global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
     const uint32_t n = P.ctl->count[depth];
-    const uint32_t* qin = P.q[depth & 1];
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t i = depth == 0 ? j : qin[j];
-        const uint32_t key = shade_key(S, P.hit_inst[i]);
+        const uint32_t key = shade_key(S, P.hit_inst[j]);
         const unsigned peers = __match_any_sync(__activemask(), key);
         const int leader = __ffs(peers) - 1;
         uint32_t base = 0;
         if (lane == leader) base = atomicAdd(&P.ctl->sort_off[key], (uint32_t)__popc(peers));
         base = __shfl_sync(peers, base, leader);
-        P.qsort[base + __popc(peers & below)] = i;
+        P.qsort[base + __popc(peers & below)] = j;  // the queue position
     }
 }
 
@@ -474,7 +475,9 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
     const bool last_was_specular = depth == 0;  // no specular BSDFs: only camera rays
     const float INF = __int_as_float(0x7f800000);
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t i = W.sort ? P.qsort[j] : (depth > 0 ? __ldcs(qin + j) : (BATCH ? j : tiled_path(W, j)));
+        // queue position of the path's ray and hit (depth 0: the path index), and the path
+        const uint32_t pos = W.sort ? P.qsort[j] : (depth > 0 ? j : (BATCH ? j : tiled_path(W, j)));
+        const uint32_t i = depth > 0 ? __ldcs(qin + pos) : pos;
         // a batch wave traces every job's camera rays; a job with max_depth 0 shades none
         if (BATCH && depth == 0 && W.jobs[P.pjob[i]].max_depth == 0) continue;
         // a camera path starts with radiance 0 and throughput 1 (integrator.rs:63-64)
@@ -521,12 +524,13 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
         const float4 bq = depth > 0 ? __ldcs(P.beta + i) : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         f3 beta = mk3(bq.x, bq.y, bq.z);
         const float last_pdf = bq.w;
-        const float4 ro = __ldcs(P.ray_o + i), rd = __ldcs(P.ray_d + i);
+        const float4 ro = __ldcs(P.ray_o[depth & 1] + pos), rd = __ldcs(P.ray_d[depth & 1] + pos);
         const f3 ray_o = mk3(ro.x, ro.y, ro.z), ray_d = mk3(rd.x, rd.y, rd.z);
         const float time = rd.w;
-        const float4 hq = __ldcs(P.hit + i);
-        const int32_t code = __ldcs(P.hit_inst + i);
+        const float4 hq = __ldcs(P.hit + pos);
+        const int32_t code = __ldcs(P.hit_inst + pos);
         bool alive = false;
+        f3 next_o, next_d;  // the next ray, written at the path's next queue position
 
         if (code == -1) {
             if (depth == 0) {  // a camera ray that escapes leaves the AOVs at zero
@@ -656,9 +660,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
                         }
                         if (survive) {
                             // Next ray (integrator.rs:377-387).
-                            f3 nd = to_world(fr, wi);
-                            P.ray_o[i] = make_float4(p_off.x, p_off.y, p_off.z, 1e-4f);
-                            P.ray_d[i] = make_float4(nd.x, nd.y, nd.z, time);
+                            next_o = p_off;
+                            next_d = to_world(fr, wi);
                             P.beta[i] = make_float4(beta.x, beta.y, beta.z, pdf_b);
                             alive = true;
                             if (ADJ) {  // for the next vertex's BSDF-sample gradient
@@ -702,8 +705,12 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
             }
         }
         P.L[i] = make_float4(L.x, L.y, L.z, 0.0f);
-        if (alive && depth + 1 < (BATCH ? W.jobs[P.pjob[i]].max_depth : W.max_depth))
-            qout[append_slot(next_count)] = i;
+        if (alive && depth + 1 < (BATCH ? W.jobs[P.pjob[i]].max_depth : W.max_depth)) {
+            const uint32_t q = append_slot(next_count);
+            qout[q] = i;
+            P.ray_o[(depth + 1) & 1][q] = make_float4(next_o.x, next_o.y, next_o.z, 1e-4f);
+            P.ray_d[(depth + 1) & 1][q] = make_float4(next_d.x, next_d.y, next_d.z, time);
+        }
     }
     if (ADJ && W.smem_grad) {  // one FP64 atomic per parameter per block
         __syncthreads();
@@ -901,8 +908,10 @@ size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* ou
                    bool adjoint = false) {
     Carver c{base};
     PathSoA s;
-    s.ray_o = c.take<float4>(P);
-    s.ray_d = c.take<float4>(P);
+    s.ray_o[0] = c.take<float4>(P);
+    s.ray_o[1] = c.take<float4>(P);
+    s.ray_d[0] = c.take<float4>(P);
+    s.ray_d[1] = c.take<float4>(P);
     s.hit = c.take<float4>(P);
     s.hit_inst = c.take<int32_t>(P);
     s.rng = c.take<uint4>(2 * P);
