@@ -322,7 +322,7 @@ struct ExtendRays {
 };
 
 // The traversal kernels ask for 9 resident blocks of 128 threads (at most 56
-// registers; k_shadow spills about 100 bytes). Warps wait mostly on node,
+// registers; k_extend spills a few dozen bytes). Warps wait mostly on node,
 // triangle and stack loads, so more of them per SM pay. On the 1080p studio
 // frame 9 blocks beat 8 (64 registers) by 2 %, and 8 beat the 7 of the
 // unconstrained 70-register build by 2 %; 10 blocks (48 registers) lose 2 %.
