@@ -148,11 +148,11 @@ __device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
 }
 
 __device__ __forceinline__ void store_rng(uint4* r, uint32_t i, const Rng& g) {
-    r[2 * (size_t)i] = make_uint4((uint32_t)g.s0, (uint32_t)(g.s0 >> 32), (uint32_t)g.s1, (uint32_t)(g.s1 >> 32));
-    r[2 * (size_t)i + 1] = make_uint4((uint32_t)g.s2, (uint32_t)(g.s2 >> 32), (uint32_t)g.s3, (uint32_t)(g.s3 >> 32));
+    __stcs(r + 2 * (size_t)i, make_uint4((uint32_t)g.s0, (uint32_t)(g.s0 >> 32), (uint32_t)g.s1, (uint32_t)(g.s1 >> 32)));
+    __stcs(r + 2 * (size_t)i + 1, make_uint4((uint32_t)g.s2, (uint32_t)(g.s2 >> 32), (uint32_t)g.s3, (uint32_t)(g.s3 >> 32)));
 }
 __device__ __forceinline__ Rng load_rng(const uint4* r, uint32_t i) {
-    uint4 a = r[2 * (size_t)i], b = r[2 * (size_t)i + 1];
+    const uint4 a = __ldcs(r + 2 * (size_t)i), b = __ldcs(r + 2 * (size_t)i + 1);
     Rng g;
     g.s0 = (uint64_t)a.x | ((uint64_t)a.y << 32);
     g.s1 = (uint64_t)a.z | ((uint64_t)a.w << 32);
@@ -288,7 +288,8 @@ __device__ __forceinline__ uint32_t tiled_path(const WaveParams& W, uint32_t j) 
 // Path state is read and written once per stage through the live-path
 // queues, so the traversal and shade kernels access it with streaming cache
 // hints (__ldcs / __stcs, evict-first); the scene's nodes and triangles keep
-// the L2 (+1.2 % on the 1080p studio frame).
+// the L2 (+1.2 % on the 1080p studio frame for the loads and hit stores,
+// +0.35 % more for shade's stores).
 // Closest hit of the live paths (Scene::intersect, scene.rs:57-97).
 template <bool BATCH>
 struct ExtendRays {
@@ -662,7 +663,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
                             // Next ray (integrator.rs:377-387).
                             next_o = p_off;
                             next_d = to_world(fr, wi);
-                            P.beta[i] = make_float4(beta.x, beta.y, beta.z, pdf_b);
+                            __stcs(P.beta + i, make_float4(beta.x, beta.y, beta.z, pdf_b));
                             alive = true;
                             if (ADJ) {  // for the next vertex's BSDF-sample gradient
                                 P.brec[3 * (size_t)i] = make_float4(wo.x, wo.y, wo.z, __uint_as_float(I.material));
@@ -696,20 +697,20 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
                     }
                     if (sh_ray) {
                         const uint32_t q = append_slot(shadow_count);
-                        P.sh_o[q] = make_float4(p_off.x, p_off.y, p_off.z, sh_tmax);
-                        P.sh_d[q] = make_float4(sh_dir.x, sh_dir.y, sh_dir.z, time);
+                        __stcs(P.sh_o + q, make_float4(p_off.x, p_off.y, p_off.z, sh_tmax));
+                        __stcs(P.sh_d + q, make_float4(sh_dir.x, sh_dir.y, sh_dir.z, time));
                         P.sq[q] = (uint32_t)sidx;
                     }
                 }
                 store_rng(P.rng, i, g);
             }
         }
-        P.L[i] = make_float4(L.x, L.y, L.z, 0.0f);
+        __stcs(P.L + i, make_float4(L.x, L.y, L.z, 0.0f));
         if (alive && depth + 1 < (BATCH ? W.jobs[P.pjob[i]].max_depth : W.max_depth)) {
             const uint32_t q = append_slot(next_count);
             qout[q] = i;
-            P.ray_o[(depth + 1) & 1][q] = make_float4(next_o.x, next_o.y, next_o.z, 1e-4f);
-            P.ray_d[(depth + 1) & 1][q] = make_float4(next_d.x, next_d.y, next_d.z, time);
+            __stcs(P.ray_o[(depth + 1) & 1] + q, make_float4(next_o.x, next_o.y, next_o.z, 1e-4f));
+            __stcs(P.ray_d[(depth + 1) & 1] + q, make_float4(next_d.x, next_d.y, next_d.z, time));
         }
     }
     if (ADJ && W.smem_grad) {  // one FP64 atomic per parameter per block
