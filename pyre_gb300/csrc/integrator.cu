@@ -242,17 +242,17 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
         float time = g.next_f32();
         f3 o, d;
         camera_ray(*cam, ndc, lens, &o, &d);
-        P.ray_o[0][i] = make_float4(o.x, o.y, o.z, 1e-4f);
-        P.ray_d[0][i] = make_float4(d.x, d.y, d.z, time);
+        __stcs(&P.ray_o[0][i], make_float4(o.x, o.y, o.z, 1e-4f));
+        __stcs(&P.ray_d[0][i], make_float4(d.x, d.y, d.z, time));
         store_rng(P.rng, i, g);
         // radiance 0, throughput 1 and the AOVs are set by shade at depth 0;
         // with max_depth 0 no vertex is shaded and the sample is all zeros
         if (max_depth == 0) {
             P.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            P.aov_a[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            P.aov_n[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            __stcs(&P.aov_a[i], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+            __stcs(&P.aov_n[i], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         }
-        for (uint32_t s = 0; s < W.ns; ++s) P.pend[(size_t)i * W.ns + s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (uint32_t s = 0; s < W.ns; ++s) __stcs(P.pend + (size_t)i * W.ns + s, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     }
 }
 
@@ -495,10 +495,10 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
         GradTerms gt;  // ADJ: this vertex's terms for the previous vertex's material
         if (depth > 0) {
             for (uint32_t s = 0; s < W.ns; ++s) {
-                float4 c = P.pend[(size_t)i * W.ns + s];
+                float4 c = __ldcs(P.pend + (size_t)i * W.ns + s);
                 if (c.w != 0.0f) {
                     L = L + mk3(c.x, c.y, c.z);
-                    P.pend[(size_t)i * W.ns + s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    __stcs(&P.pend[(size_t)i * W.ns + s], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
                     if (ADJ) collect_parked_grad(P.gpend + PYRE_GSLOT * ((size_t)i * W.ns + s), gt);
                 }
             }
@@ -535,8 +535,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
 
         if (code == -1) {
             if (depth == 0) {  // a camera ray that escapes leaves the AOVs at zero
-                P.aov_a[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                P.aov_n[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                __stcs(&P.aov_a[i], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+                __stcs(&P.aov_n[i], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
             }
             // Escaped: environment radiance with MIS against the BSDF arm (integrator.rs:243-259).
             if (S.has_env) {
@@ -559,8 +559,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
             // Quad light hit (integrator.rs:262-295).
             const DevQuadLight& Lt = S.lights[-2 - code];
             if (depth == 0) {
-                P.aov_a[i] = make_float4(1.0f, 1.0f, 1.0f, hq.x);
-                P.aov_n[i] = make_float4(Lt.normal.x, Lt.normal.y, Lt.normal.z, 0.0f);
+                __stcs(&P.aov_a[i], make_float4(1.0f, 1.0f, 1.0f, hq.x));
+                __stcs(&P.aov_n[i], make_float4(Lt.normal.x, Lt.normal.y, Lt.normal.z, 0.0f));
             }
             f3 le = dot3(Lt.normal, -ray_d) > 0.0f ? Lt.emission : splat3(0.0f);
             if (last_was_specular) L = L + beta * le;
@@ -595,8 +595,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
             }
             const Bsdf mat = load_bsdf(S, I.material);
             if (depth == 0) {
-                P.aov_a[i] = make_float4(mat.base.x, mat.base.y, mat.base.z, t);
-                P.aov_n[i] = make_float4(ns.x, ns.y, ns.z, 0.0f);
+                __stcs(&P.aov_a[i], make_float4(mat.base.x, mat.base.y, mat.base.z, t));
+                __stcs(&P.aov_n[i], make_float4(ns.x, ns.y, ns.z, 0.0f));
             }
             const Frame3 fr = frame_from_normal(ns);
             const f3 wo = to_local(fr, -ray_d);
@@ -677,7 +677,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
                     const float w = power_heuristic(lpdf, pdf_b);
                     const f3 contrib = beta * f * le * wi.z * w / lpdf;
                     const size_t sidx = (size_t)i * W.ns + (env_arm ? S.n_lights : s);
-                    P.pend[sidx] = make_float4(contrib.x, contrib.y, contrib.z, 1.0f);
+                    __stcs(&P.pend[sidx], make_float4(contrib.x, contrib.y, contrib.z, 1.0f));
                     if (ADJ) {  // park the slot's d/d params (and texels); cleared if occluded
                         float4* G = P.gpend + PYRE_GSLOT * sidx;
                         float gm[6];
@@ -754,10 +754,10 @@ __global__ void k_accumulate(PathSoA P, WaveParams W) {
             mean = mk3(W.prog_mean[3 * (size_t)p], W.prog_mean[3 * (size_t)p + 1], W.prog_mean[3 * (size_t)p + 2]);
         for (uint32_t k = 0; k < kv; ++k) {
             uint32_t i = k * W.npix + p;
-            float4 Lq = P.L[i];
+            const float4 Lq = __ldcs(P.L + i);  // last reads of the path state
             f3 L = mk3(Lq.x, Lq.y, Lq.z);
             for (uint32_t s = 0; s < W.ns; ++s) {
-                float4 c = P.pend[(size_t)i * W.ns + s];
+                const float4 c = __ldcs(P.pend + (size_t)i * W.ns + s);
                 if (c.w != 0.0f) L = L + mk3(c.x, c.y, c.z);
             }
             if (W.prog_mean) {
@@ -765,7 +765,7 @@ __global__ void k_accumulate(PathSoA P, WaveParams W) {
                 const float n = (float)(P.ctl->s_base + k + 1);
                 mean = mean + (L - mean) / n;
             }
-            float4 a = P.aov_a[i], nn = P.aov_n[i];
+            const float4 a = __ldcs(P.aov_a + i), nn = __ldcs(P.aov_n + i);
             ar.x += L.x; ar.y += L.y; ar.z += L.z; ar.w += a.w;
             aa.x += a.x; aa.y += a.y; aa.z += a.z;
             an.x += nn.x; an.y += nn.y; an.z += nn.z;
