@@ -530,8 +530,6 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
         const float time = rd.w;
         const float4 hq = __ldcs(P.hit + pos);
         const int32_t code = __ldcs(P.hit_inst + pos);
-        bool alive = false;
-        f3 next_o, next_d;  // the next ray, written at the path's next queue position
 
         if (code == -1) {
             if (depth == 0) {  // a camera ray that escapes leaves the AOVs at zero
@@ -660,11 +658,16 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
                             else beta = beta / (1.0f - q);
                         }
                         if (survive) {
-                            // Next ray (integrator.rs:377-387).
-                            next_o = p_off;
-                            next_d = to_world(fr, wi);
+                            // Next ray (integrator.rs:377-387), at the path's
+                            // position in the next depth's queue
+                            if (depth + 1 < (BATCH ? W.jobs[P.pjob[i]].max_depth : W.max_depth)) {
+                                const f3 nd = to_world(fr, wi);
+                                const uint32_t q = append_slot(next_count);
+                                qout[q] = i;
+                                __stcs(P.ray_o[(depth + 1) & 1] + q, make_float4(p_off.x, p_off.y, p_off.z, 1e-4f));
+                                __stcs(P.ray_d[(depth + 1) & 1] + q, make_float4(nd.x, nd.y, nd.z, time));
+                            }
                             __stcs(P.beta + i, make_float4(beta.x, beta.y, beta.z, pdf_b));
-                            alive = true;
                             if (ADJ) {  // for the next vertex's BSDF-sample gradient
                                 P.brec[3 * (size_t)i] = make_float4(wo.x, wo.y, wo.z, __uint_as_float(I.material));
                                 P.brec[3 * (size_t)i + 1] = make_float4(wi.x, wi.y, wi.z, 1.0f);
@@ -706,12 +709,6 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WavePar
             }
         }
         __stcs(P.L + i, make_float4(L.x, L.y, L.z, 0.0f));
-        if (alive && depth + 1 < (BATCH ? W.jobs[P.pjob[i]].max_depth : W.max_depth)) {
-            const uint32_t q = append_slot(next_count);
-            qout[q] = i;
-            __stcs(P.ray_o[(depth + 1) & 1] + q, make_float4(next_o.x, next_o.y, next_o.z, 1e-4f));
-            __stcs(P.ray_d[(depth + 1) & 1] + q, make_float4(next_d.x, next_d.y, next_d.z, time));
-        }
     }
     if (ADJ && W.smem_grad) {  // one FP64 atomic per parameter per block
         __syncthreads();
