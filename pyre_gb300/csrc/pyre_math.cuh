@@ -88,7 +88,9 @@ struct Rng {
     PYRE_HD void seed(uint64_t seed) {
         uint64_t x = seed;
         uint64_t st[4];
+#ifdef __CUDA_ARCH__
 #pragma unroll
+#endif
         for (int i = 0; i < 4; ++i) {
             x += 0x9E3779B97F4A7C15ull;
             uint64_t z = x;
