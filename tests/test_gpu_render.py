@@ -82,6 +82,24 @@ def test_crop_and_sample_range_resume(gpu_ctx, oracle_mod):
     np.testing.assert_array_equal(g.radiance, full.radiance)
 
 
+@pytest.mark.parametrize("crop", [(3, 5, 8, 7), (0, 0, 64, 1), (17, 0, 18, 64), (8, 4, 16, 8), (1, 1, 63, 62)])
+def test_odd_crops_match_the_full_frame(gpu_ctx, crop):
+    """Crops narrower than a camera tile (8 px), shorter than a tile band
+    (4 rows), a single row or column, or with partial tiles on both edges
+    give the full frame's pixels bit for bit (the depth-0 tile order is a
+    bijection for every crop shape)."""
+    sc, cam = P.cornell_box(), P.cornell_box_camera(64, 64)
+    ds = gpu_ctx.upload(sc)
+    it = PathIntegrator(8, 3)
+    full = gpu_ctx.render(ds, cam, it, 64, 64, 3)
+    x0, y0, x1, y1 = crop
+    c = gpu_ctx.render(ds, cam, it, 64, 64, 3, crop=crop)
+    np.testing.assert_array_equal(c.radiance, full.radiance[y0:y1, x0:x1])
+    np.testing.assert_array_equal(c.albedo, full.albedo[y0:y1, x0:x1])
+    np.testing.assert_array_equal(c.depth, full.depth[y0:y1, x0:x1])
+    ds.close()
+
+
 def test_procedural_studio_small(gpu_ctx, oracle_mod):
     sc = P.studio_procedural(n_side=3, segments=24, n_moving=2, hdri_size=(256, 128))
     cam = P.studio_procedural_camera(160, 90)
