@@ -263,7 +263,9 @@ typedef struct pyre_render_params {
     uint32_t env_sampling;           /* PYRE_ENV_ALIAS or PYRE_ENV_CDF */
     uint32_t wave_paths;             /* paths in flight per wave; 0 = automatic (what a quarter
                                         of the free device memory holds, 8 Mi to 128 Mi) */
-    uint32_t block_size;             /* threads per block of the stage kernels; 0 = 256 */
+    uint32_t block_size;             /* threads per block of the stage kernels (at most 224
+                                        for the forward shade, 128 for the traversals);
+                                        0 = 256 / 224 / 128 */
     uint32_t sort_by_material;       /* reorder the shade queue by material */
     uint32_t use_graph;              /* capture one wave as a CUDA graph and replay it */
     uint32_t refill_lanes;           /* traversal: refetch rays once this many lanes of a

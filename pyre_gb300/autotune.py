@@ -1,8 +1,9 @@
 """Autotuner for the wavefront's launch knobs.
 
 Knobs (pyre_render_params): wave_paths (queue capacity = paths in flight per
-wave), block_size (threads per block of the shade-type kernels; the trace
-kernels use min(block_size, 128)), use_graph (CUDA-graph replay),
+wave), block_size (threads per block of the stage kernels, capped at 224 for
+the forward shade and 128 for the traversals; 0 = the library's defaults
+256 / 224 / 128), use_graph (CUDA-graph replay),
 sort_by_material (shade visits the live paths sorted by material) and
 refill_lanes (a warp refetches rays once this many of its lanes are idle) and
 bvh_width (instance BVHs traversed as binary, 4-wide or 8-wide nodes).
@@ -21,13 +22,13 @@ from pathlib import Path
 
 KNOBS = {
     "wave_paths": [0, 8 << 20, 32 << 20, 128 << 20],  # 0: the library's memory-based choice
-    "block_size": [128, 256],
+    "block_size": [0, 128],  # 0: the library's defaults
     "use_graph": [0, 1],
     "bvh_width": [2, 4, 8],
     "sort_by_material": [0, 1],
     "refill_lanes": [0, 4, 8, 16, 32],  # 0: the library's defaults (16 closest hit, 8 any hit)
 }
-DEFAULT = {"wave_paths": 0, "block_size": 256, "use_graph": 0, "bvh_width": 2, "sort_by_material": 0,
+DEFAULT = {"wave_paths": 0, "block_size": 0, "use_graph": 0, "bvh_width": 2, "sort_by_material": 0,
            "refill_lanes": 0}
 
 

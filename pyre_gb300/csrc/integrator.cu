@@ -461,8 +461,13 @@ __global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
 // One path vertex of PathIntegrator::integrate (integrator.rs:242-388).
 // ADJ: the path-replay adjoint of the same vertex (pyre_backward): the same
 // draws and decisions, plus the derivatives of its terms.
+// Forward shade: 4 resident blocks of 224 threads (72 registers); it is
+// latency-bound, and 28 warps per SM beat 24 (3 blocks of 256, 80
+// registers) by 0.3 % on the 1080p studio frame. The adjoint variant keeps
+// 3 blocks of 256: at 72 registers its spills would grow.
 template <bool BATCH, bool ADJ = false>
-__global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+__global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene S, PathSoA P, WaveParams W,
+                                                                        uint32_t depth) {
     extern __shared__ double sgrad[];
     if (ADJ && W.smem_grad) {
         for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x) sgrad[k] = 0.0;
@@ -955,23 +960,26 @@ uint64_t default_wave_paths(pyre_ctx* ctx, uint32_t ns, bool batch, bool adjoint
 }
 
 struct Launch {
-    int block_shade = 256;  // raygen, shade, accumulate (at most 256)
+    int block_stage = 256;  // raygen, accumulate, adjoint shade (at most 256)
+    int block_shade = 224;  // forward shade (at most 224)
     int block_trace = 128;  // extend, shadow (at most 128)
     int grid_raygen, grid_shade, grid_extend, grid_shadow, grid_acc, grid_sort;
 };
 
 // Grid sizes for the stage kernels: persistent grids of resident blocks.
-// block_size (0 = defaults 256/128) sets the shade-type blocks; the trace
-// kernels use min(block_size, 128).
+// block_size (0 = defaults: 256 for raygen and accumulate, 224 for the
+// forward shade, 128 for the traces) sets them all, capped at 224 for the
+// forward shade and 128 for the traces.
 template <bool BATCH>
 Launch make_launch(pyre_ctx* ctx, uint32_t block_size, int width) {
     Launch L;
     if (block_size) {
         const int b = (int)std::max(32u, std::min(256u, block_size / 32 * 32));
-        L.block_shade = b;
+        L.block_stage = b;
+        L.block_shade = std::min(b, 224);
         L.block_trace = std::min(b, 128);
     }
-    L.grid_raygen = grid_for(ctx, k_raygen<BATCH>, L.block_shade);
+    L.grid_raygen = grid_for(ctx, k_raygen<BATCH>, L.block_stage);
     L.grid_shade = grid_for(ctx, k_shade<BATCH>, L.block_shade);
     L.grid_extend = width == 8 ? grid_for(ctx, k_extend<BATCH, 8>, L.block_trace)
                     : width == 4 ? grid_for(ctx, k_extend<BATCH, 4>, L.block_trace)
@@ -979,7 +987,7 @@ Launch make_launch(pyre_ctx* ctx, uint32_t block_size, int width) {
     L.grid_shadow = width == 8 ? grid_for(ctx, k_shadow<BATCH, 8>, L.block_trace)
                     : width == 4 ? grid_for(ctx, k_shadow<BATCH, 4>, L.block_trace)
                                  : grid_for(ctx, k_shadow<BATCH, 2>, L.block_trace);
-    L.grid_acc = BATCH ? grid_for(ctx, k_accumulate_batch, L.block_shade) : grid_for(ctx, k_accumulate, L.block_shade);
+    L.grid_acc = BATCH ? grid_for(ctx, k_accumulate_batch, L.block_stage) : grid_for(ctx, k_accumulate, L.block_stage);
     L.grid_sort = grid_for(ctx, k_sort_scatter, 256);
     return L;
 }
@@ -1028,7 +1036,7 @@ void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Wave
     cudaStream_t st = ctx->stream;
     mark(ctx, STAGE_OTHER);
     k_wave_begin<<<1, 32, 0, st>>>(P.ctl, W.spp_begin, W.spp_end, W.k_per_wave, W.npix);
-    k_raygen<false><<<Lc.grid_raygen, Lc.block_shade, 0, st>>>(P, W);
+    k_raygen<false><<<Lc.grid_raygen, Lc.block_stage, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
         launch_extend<false>(st, Lc, S, P, W, d);
@@ -1041,7 +1049,7 @@ void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Wave
         }
     }
     mark(ctx, STAGE_OTHER);
-    k_accumulate<<<Lc.grid_acc, Lc.block_shade, 0, st>>>(P, W);
+    k_accumulate<<<Lc.grid_acc, Lc.block_stage, 0, st>>>(P, W);
     k_wave_end<<<1, 32, 0, st>>>(P.ctl, W.max_depth);
     mark(ctx, STAGE_END);
 }
@@ -1052,7 +1060,7 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
     cudaStream_t st = ctx->stream;
     mark(ctx, STAGE_OTHER);
     k_wave_begin_batch<<<1, 32, 0, st>>>(P.ctl, W.waves);
-    k_raygen<true><<<Lc.grid_raygen, Lc.block_shade, 0, st>>>(P, W);
+    k_raygen<true><<<Lc.grid_raygen, Lc.block_stage, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
         launch_extend<true>(st, Lc, S, P, W, d);
@@ -1065,7 +1073,7 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
         }
     }
     mark(ctx, STAGE_OTHER);
-    k_accumulate_batch<<<Lc.grid_acc, Lc.block_shade, 0, st>>>(P, W);
+    k_accumulate_batch<<<Lc.grid_acc, Lc.block_stage, 0, st>>>(P, W);
     k_wave_end<<<1, 32, 0, st>>>(P.ctl, W.max_depth);
     mark(ctx, STAGE_END);
 }
@@ -1194,7 +1202,7 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
                       W.min_rr, W.ns, W.spp_begin, W.spp_end, W.cx0 + W.cy0 * 65536u, W.env_cdf, W.refill, W.sort,
                       W.bvh_width);
         std::string k2 = std::string(key) + "/" + std::to_string(W.width) + "x" + std::to_string(W.height) + "/b" +
-                         std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace);
+                         std::to_string(Lc.block_stage) + "x" + std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace);
         // camera bytes are part of the key
         k2.append(reinterpret_cast<const char*>(&W.cam), sizeof(W.cam));
         if (!ctx->wave_graph || ctx->wave_graph_key != k2) {
@@ -1379,7 +1387,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
         std::string key = "batch/" + std::to_string(scene->serial) + "/" +
                           std::to_string((uintptr_t)ctx->render_ws.ptr) + "/" + std::to_string(n_waves) + "/" +
                           std::to_string(max_depth) + "/" + std::to_string(max_paths) + "/b" +
-                          std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace) + "/r" +
+                          std::to_string(Lc.block_stage) + "x" + std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace) + "/r" +
                           std::to_string(W.refill) + "/s" + std::to_string(W.sort) + "/w" + std::to_string(W.bvh_width) +
                           "/";
         key.append(reinterpret_cast<const char*>(dj.data()), job_bytes);
@@ -1778,20 +1786,20 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     W.smem_grad = smem ? 1 : 0;
 
     const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
-    const int grid_adj = grid_for(ctx, k_shade<false, true>, Lc.block_shade, smem);
-    const int grid_acc = grid_for(ctx, k_accumulate_adjoint, Lc.block_shade, smem);
+    const int grid_adj = grid_for(ctx, k_shade<false, true>, Lc.block_stage, smem);
+    const int grid_acc = grid_for(ctx, k_accumulate_adjoint, Lc.block_stage, smem);
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
     PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
     for (uint32_t w = 0; w < waves; ++w) {
         k_wave_begin<<<1, 32, 0, st>>>(S.ctl, W.spp_begin, W.spp_end, W.k_per_wave, W.npix);
-        k_raygen<false><<<Lc.grid_raygen, Lc.block_shade, 0, st>>>(S, W);
+        k_raygen<false><<<Lc.grid_raygen, Lc.block_stage, 0, st>>>(S, W);
         for (uint32_t d = 0; d < W.max_depth; ++d) {
             launch_extend<false>(st, Lc, D, S, W, d);
             if (W.sort) enqueue_sort(ctx, D, S, Lc, d);
-            k_shade<false, true><<<grid_adj, Lc.block_shade, smem, st>>>(D, S, W, d);
+            k_shade<false, true><<<grid_adj, Lc.block_stage, smem, st>>>(D, S, W, d);
             if (W.ns > 0) launch_shadow<false>(st, Lc, D, S, W, d);
         }
-        k_accumulate_adjoint<<<grid_acc, Lc.block_shade, smem, st>>>(D, S, W);
+        k_accumulate_adjoint<<<grid_acc, Lc.block_stage, smem, st>>>(D, S, W);
         k_wave_end<<<1, 32, 0, st>>>(S.ctl, W.max_depth);
     }
     PYRE_CUDA_TRY(ctx, cudaGetLastError());
