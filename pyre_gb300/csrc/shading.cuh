@@ -305,7 +305,6 @@ __device__ __forceinline__ f3 env_texture(const DevEnv& E, f2 uv) {  // light.rs
     f3 p00 = env_texel(E, x0, y0), p10 = env_texel(E, x1, y0), p01 = env_texel(E, x0, y1), p11 = env_texel(E, x1, y1);
     return p00 * ((1.0f - dx) * (1.0f - dy)) + p10 * (dx * (1.0f - dy)) + p01 * ((1.0f - dx) * dy) + p11 * (dx * dy);
 }
-__device__ __forceinline__ f3 env_le(const DevEnv& E, f3 wi) { return env_texture(E, env_dir_to_uv(wi)) * E.intensity; }
 
 // Distribution2D::pdf_at (distribution.rs:157-163) from per-bin pdf tables
 // holding (cdf[b+1]-cdf[b])*n exactly as Distribution1D::pdf_at computes it.
@@ -323,7 +322,6 @@ __device__ __forceinline__ float env_pdf_at(const DevEnv& E, f2 uv) {
     if (st < 1e-6f) return 0.0f;
     return env_pdf_uv(E, uv) / (2.0f * PYRE_PI * PYRE_PI * st);
 }
-__device__ __forceinline__ float env_pdf(const DevEnv& E, f3 wi) { return env_pdf_at(E, env_dir_to_uv(wi)); }
 
 // Distribution1D::sample_continuous (distribution.rs:79-101) over a CDF row.
 __device__ __forceinline__ float cdf_sample(const float* cdf, uint32_t n, float u, float* pdf, uint32_t* bin_out) {
