@@ -235,7 +235,8 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
     constexpr int STACK = WIDTH == 8 ? 96 : PYRE_STACK;
     // Any-hit traversal keeps the bottom 8 stack entries of each lane in
     // shared memory (entry-major, so a lane always uses its own bank), the
-    // rest in local memory: the shadow stage is 4 % faster on the 1080p frame.
+    // rest in local memory: the shadow stage is 4 % faster on the 1080p frame
+    // (4 or 12 entries are slower than 8).
     // Closest hit keeps the whole stack in local memory; with the same short
     // stack it was 0.6 % slower (4 entries), 2 % (8) and 4 % (16).
     constexpr int SK = ANY ? 8 : 0;
