@@ -148,8 +148,10 @@ __device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
 }
 
 __device__ __forceinline__ void store_rng(uint4* r, uint32_t i, const Rng& g) {
-    __stcs(r + 2 * (size_t)i, make_uint4((uint32_t)g.s0, (uint32_t)(g.s0 >> 32), (uint32_t)g.s1, (uint32_t)(g.s1 >> 32)));
-    __stcs(r + 2 * (size_t)i + 1, make_uint4((uint32_t)g.s2, (uint32_t)(g.s2 >> 32), (uint32_t)g.s3, (uint32_t)(g.s3 >> 32)));
+    __stcs(r + 2 * (size_t)i,
+           make_uint4((uint32_t)g.s0, (uint32_t)(g.s0 >> 32), (uint32_t)g.s1, (uint32_t)(g.s1 >> 32)));
+    __stcs(r + 2 * (size_t)i + 1,
+           make_uint4((uint32_t)g.s2, (uint32_t)(g.s2 >> 32), (uint32_t)g.s3, (uint32_t)(g.s3 >> 32)));
 }
 __device__ __forceinline__ Rng load_rng(const uint4* r, uint32_t i) {
     const uint4 a = __ldcs(r + 2 * (size_t)i), b = __ldcs(r + 2 * (size_t)i + 1);
@@ -1202,7 +1204,8 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
                       W.min_rr, W.ns, W.spp_begin, W.spp_end, W.cx0 + W.cy0 * 65536u, W.env_cdf, W.refill, W.sort,
                       W.bvh_width);
         std::string k2 = std::string(key) + "/" + std::to_string(W.width) + "x" + std::to_string(W.height) + "/b" +
-                         std::to_string(Lc.block_stage) + "x" + std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace);
+                         std::to_string(Lc.block_stage) + "x" + std::to_string(Lc.block_shade) + "x" +
+                         std::to_string(Lc.block_trace);
         // camera bytes are part of the key
         k2.append(reinterpret_cast<const char*>(&W.cam), sizeof(W.cam));
         if (!ctx->wave_graph || ctx->wave_graph_key != k2) {
@@ -1387,7 +1390,8 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
         std::string key = "batch/" + std::to_string(scene->serial) + "/" +
                           std::to_string((uintptr_t)ctx->render_ws.ptr) + "/" + std::to_string(n_waves) + "/" +
                           std::to_string(max_depth) + "/" + std::to_string(max_paths) + "/b" +
-                          std::to_string(Lc.block_stage) + "x" + std::to_string(Lc.block_shade) + "x" + std::to_string(Lc.block_trace) + "/r" +
+                          std::to_string(Lc.block_stage) + "x" + std::to_string(Lc.block_shade) + "x" +
+                          std::to_string(Lc.block_trace) + "/r" +
                           std::to_string(W.refill) + "/s" + std::to_string(W.sort) + "/w" + std::to_string(W.bvh_width) +
                           "/";
         key.append(reinterpret_cast<const char*>(dj.data()), job_bytes);
