@@ -1,0 +1,60 @@
+"""The ctypes mirror of include/pyre_cuda.h has the C structs' layout: a C
+program compiled against the header prints every struct's size and every
+field's offset, and each must equal the ctypes class's."""
+import ctypes as C
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from pyre_gb300 import native as N
+
+ROOT = Path(__file__).resolve().parents[1]
+
+PAIRS = {
+    "pyre_bvh2_node": N.Bvh2Node,
+    "pyre_mesh_desc": N.MeshDesc,
+    "pyre_instance_desc": N.InstanceDesc,
+    "pyre_material_desc": N.MaterialDesc,
+    "pyre_quad_light_desc": N.QuadLightDesc,
+    "pyre_env_desc": N.EnvDesc,
+    "pyre_scene_desc": N.SceneDesc,
+    "pyre_scene_info": N.SceneInfo,
+    "pyre_rays": N.Rays,
+    "pyre_hits": N.Hits,
+    "pyre_camera_desc": N.CameraDesc,
+    "pyre_render_params": N.RenderParams,
+    "pyre_film": N.Film,
+    "pyre_render_stats": N.RenderStats,
+    "pyre_gradients": N.Gradients,
+    "pyre_batch_job": N.BatchJob,
+}
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "pyre_cuda.h"', "int main(void) {"]
+    for cname, cls in PAIRS.items():
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in cls._fields_:
+            lines.append(f'    printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run([cc, "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    c_layout = {}
+    for line in out:
+        if line:
+            cname, what, value = line.split()
+            c_layout[(cname, what)] = int(value)
+    for cname, cls in PAIRS.items():
+        assert C.sizeof(cls) == c_layout[(cname, "size")], cname
+        for field, _ in cls._fields_:
+            assert getattr(cls, field).offset == c_layout[(cname, field)], (cname, field)
