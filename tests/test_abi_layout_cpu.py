@@ -58,3 +58,15 @@ def test_ctypes_structs_match_the_header(tmp_path):
         assert C.sizeof(cls) == c_layout[(cname, "size")], cname
         for field, _ in cls._fields_:
             assert getattr(cls, field).offset == c_layout[(cname, field)], (cname, field)
+
+
+def test_python_constants_match_the_header():
+    """Every PYRE_* value the header defines and native.py mirrors is equal."""
+    import re
+    text = (ROOT / "include" / "pyre_cuda.h").read_text()
+    defines = {m.group(1): int(m.group(2)) for m in
+               re.finditer(r"^#define (PYRE_[A-Z0-9_]+) (-?\d+)\b", text, re.M)}
+    mirrored = {name: getattr(N, name) for name in defines if hasattr(N, name)}
+    assert len(mirrored) >= 15
+    for name, value in mirrored.items():
+        assert value == defines[name], name
