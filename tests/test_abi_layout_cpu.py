@@ -70,3 +70,34 @@ def test_python_constants_match_the_header():
     assert len(mirrored) >= 15
     for name, value in mirrored.items():
         assert value == defines[name], name
+
+
+def _c_struct_fields(header: str) -> dict:
+    import re
+    out = {}
+    for m in re.finditer(r"typedef struct (pyre_\w+) \{(.*?)\} \1;", header, re.S):
+        body = re.sub(r"/\*.*?\*/", "", m.group(2), flags=re.S)
+        fields = []
+        for decl in body.split(";"):
+            decl = re.sub(r"\[[^\]]*\]", "", decl.strip())
+            if not decl:
+                continue
+            parts = decl.split(",")
+            fields.append(parts[0].split()[-1].lstrip("*"))
+            fields += [q.strip().lstrip("*") for q in parts[1:]]
+        out[m.group(1)] = fields
+    return out
+
+
+def test_rust_binding_sketch_matches_the_header():
+    """The #[repr(C)] structs of the Rust binding in INTEGRATION.md list the
+    C structs' fields in the same order (no Rust compiler checks them here)."""
+    import re
+    doc = (ROOT / "INTEGRATION.md").read_text()
+    cs = _c_struct_fields((ROOT / "include" / "pyre_cuda.h").read_text())
+    rust = {m.group(1): re.findall(r"pub (\w+):", m.group(2))
+            for m in re.finditer(r"#\[repr\(C\)\] pub struct (\w+) \{(.*?)\}", doc, re.S)}
+    assert len(rust) >= 16
+    for name, fields in rust.items():
+        cname = "pyre_" + re.sub(r"(?<!^)(?=[A-Z])", "_", name[len("Pyre"):]).lower()
+        assert cs.get(cname) == fields, (name, fields, cs.get(cname))
