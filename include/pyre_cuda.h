@@ -397,8 +397,9 @@ int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const pyre_batch_j
  * must be caller-owned device memory (film->mem == PYRE_MEM_DEVICE).
  * Limits: the crop (x1-x0)*(y1-y0) must fit the array with one sample per
  * pixel (PYRE_ERR_INVALID names the largest pixel count for the scene's light
- * count otherwise); render larger images as crop tiles. No CUDA graph
- * replay; stage timing is ignored.
+ * count otherwise); render larger images as crop tiles. The wave size
+ * (wave_paths, 0 = 8 Mi paths) is lowered until a wave fits the array.
+ * params->use_graph and stage timing are ignored; the other knobs apply.
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call
  * before any stream capture. Every call on a device shares the one array and

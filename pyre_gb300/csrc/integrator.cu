@@ -1084,6 +1084,28 @@ uint32_t kernels_per_wave(const WaveParams& W) {
     return 4 + W.max_depth * ((W.ns > 0 ? 3 : 2) + (W.sort ? 3 : 0));
 }
 
+// Largest pixel count of one view: path and pixel indices are 32-bit, and a
+// wave holds at least one sample of every pixel.
+#define PYRE_MAX_PIXELS (1ull << 31)
+
+// The crop of the render parameters (all zero = the whole image) as
+// c = {x0, y0, x1, y1} and its pixel count, computed in 64 bits: crops outside
+// the image, empty crops and crops above PYRE_MAX_PIXELS are rejected before
+// anything divides by the count.
+int resolve_crop(pyre_ctx* ctx, const pyre_render_params& rp, const char* who, uint32_t c[4], uint32_t* npix) {
+    if (rp.width == 0 || rp.height == 0) return set_error(ctx, PYRE_ERR_INVALID, std::string(who) + ": image size is zero");
+    c[0] = rp.crop[0]; c[1] = rp.crop[1]; c[2] = rp.crop[2]; c[3] = rp.crop[3];
+    if (c[0] == 0 && c[1] == 0 && c[2] == 0 && c[3] == 0) { c[2] = rp.width; c[3] = rp.height; }
+    if (c[2] > rp.width || c[3] > rp.height || c[0] >= c[2] || c[1] >= c[3])
+        return set_error(ctx, PYRE_ERR_INVALID, std::string(who) + ": crop outside the image");
+    const uint64_t n = (uint64_t)(c[2] - c[0]) * (uint64_t)(c[3] - c[1]);
+    if (n == 0 || n > PYRE_MAX_PIXELS)
+        return set_error(ctx, PYRE_ERR_INVALID, std::string(who) + ": crop of " + std::to_string(n) +
+                                                    " pixels (at most 2^31 per view)");
+    *npix = (uint32_t)n;
+    return PYRE_OK;
+}
+
 }  // namespace
 }  // namespace pyre
 
@@ -1107,18 +1129,16 @@ int pyre_render_progressive(pyre_ctx* ctx, const pyre_scene* scene, const pyre_c
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_progressive: NULL argument");
     if (mem != PYRE_MEM_HOST && mem != PYRE_MEM_DEVICE)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_progressive: mem must be PYRE_MEM_HOST or PYRE_MEM_DEVICE");
-    const pyre_render_params& rp = *params;
-    uint32_t x0 = rp.crop[0], y0 = rp.crop[1], x1 = rp.crop[2], y1 = rp.crop[3];
-    if (x0 == 0 && y0 == 0 && x1 == 0 && y1 == 0) { x1 = rp.width; y1 = rp.height; }
-    if (x1 > rp.width || y1 > rp.height || x0 >= x1 || y0 >= y1)
-        return set_error(ctx, PYRE_ERR_INVALID, "crop outside the image");
+    uint32_t c[4], npix = 0;
+    int rc = resolve_crop(ctx, *params, "pyre_render_progressive", c, &npix);
+    if (rc) return rc;
     cudaSetDevice(ctx->device);
     pyre_film none;
     std::memset(&none, 0, sizeof none);
     none.mem = PYRE_MEM_DEVICE;
     if (mem == PYRE_MEM_DEVICE) return render_impl(ctx, scene, camera, params, &none, nullptr, mean_rgb);
-    const size_t bytes = (size_t)(x1 - x0) * (y1 - y0) * 3 * sizeof(float);
-    int rc = ensure_workspace(ctx, ctx->prog_ws, bytes);
+    const size_t bytes = (size_t)npix * 3 * sizeof(float);
+    rc = ensure_workspace(ctx, ctx->prog_ws, bytes);
     if (rc) return rc;
     float* d = (float*)ctx->prog_ws.ptr;
     PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(d, mean_rgb, bytes, cudaMemcpyHostToDevice, ctx->stream));
@@ -1140,13 +1160,11 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_render: NULL argument");
     cudaSetDevice(ctx->device);
     const pyre_render_params& rp = *params;
-    if (rp.width == 0 || rp.height == 0) return set_error(ctx, PYRE_ERR_INVALID, "image size is zero");
+    uint32_t c[4], npix = 0;
+    int rc = resolve_crop(ctx, rp, "pyre_render", c, &npix);
+    if (rc) return rc;
     if (rp.spp_end <= rp.spp_begin) return set_error(ctx, PYRE_ERR_INVALID, "empty sample range");
     if (rp.max_depth > PYRE_MAX_DEPTH) return set_error(ctx, PYRE_ERR_INVALID, "max_depth above 64");
-    uint32_t x0 = rp.crop[0], y0 = rp.crop[1], x1 = rp.crop[2], y1 = rp.crop[3];
-    if (x0 == 0 && y0 == 0 && x1 == 0 && y1 == 0) { x1 = rp.width; y1 = rp.height; }
-    if (x1 > rp.width || y1 > rp.height || x0 >= x1 || y0 >= y1)
-        return set_error(ctx, PYRE_ERR_INVALID, "crop outside the image");
     if (camera->kind > PYRE_CAMERA_THIN_LENS) return set_error(ctx, PYRE_ERR_INVALID, "unknown camera kind");
     if (film->mem != PYRE_MEM_HOST && film->mem != PYRE_MEM_DEVICE)
         return set_error(ctx, PYRE_ERR_INVALID, "film.mem must be PYRE_MEM_HOST or PYRE_MEM_DEVICE");
@@ -1155,8 +1173,8 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     std::memset(&W, 0, sizeof W);
     W.cam = make_camera(*camera);
     W.width = rp.width; W.height = rp.height;
-    W.cx0 = x0; W.cy0 = y0; W.cw = x1 - x0; W.ch = y1 - y0;
-    W.npix = W.cw * W.ch;
+    W.cx0 = c[0]; W.cy0 = c[1]; W.cw = c[2] - c[0]; W.ch = c[3] - c[1];
+    W.npix = npix;
     W.spp_begin = rp.spp_begin; W.spp_end = rp.spp_end;
     W.max_depth = rp.max_depth; W.min_rr = rp.min_rr_depth;
     W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
@@ -1166,7 +1184,7 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     W.sort = rp.sort_by_material ? 1 : 0;
     W.prog_mean = prog;
     DevScene D;
-    int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width);
+    rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width);
     if (rc) return rc;
     const uint32_t spp = rp.spp_end - rp.spp_begin;
     uint64_t target = rp.wave_paths ? rp.wave_paths : default_wave_paths(ctx, W.ns, false, false);
@@ -1298,8 +1316,10 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
         DevJob& d = dj[j];
         std::memset(&d, 0, sizeof d);
         d.cam = make_camera(jb.camera);
+        if ((uint64_t)jb.width * jb.height > PYRE_MAX_PIXELS)
+            return set_error(ctx, PYRE_ERR_INVALID, tag + "more than 2^31 pixels");
         d.width = jb.width; d.height = jb.height;
-        d.npix = jb.width * jb.height;
+        d.npix = (uint32_t)((uint64_t)jb.width * jb.height);
         d.spp_begin = jb.spp_begin; d.spp_end = jb.spp_end;
         d.max_depth = jb.max_depth; d.min_rr = jb.min_rr_depth;
         d.tlas_root = scene->part_tlas[jb.part];
@@ -1477,21 +1497,19 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     const pyre_render_params& rp = *params;
     if (film->mem != PYRE_MEM_DEVICE)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_render_noalloc: the film must be device memory");
-    if (rp.width == 0 || rp.height == 0) return set_error(ctx, PYRE_ERR_INVALID, "image size is zero");
+    uint32_t c[4], npix = 0;
+    int rc = resolve_crop(ctx, rp, "pyre_render_noalloc", c, &npix);
+    if (rc) return rc;
     if (rp.spp_end <= rp.spp_begin) return set_error(ctx, PYRE_ERR_INVALID, "empty sample range");
     if (rp.max_depth > PYRE_MAX_DEPTH) return set_error(ctx, PYRE_ERR_INVALID, "max_depth above 64");
-    uint32_t x0 = rp.crop[0], y0 = rp.crop[1], x1 = rp.crop[2], y1 = rp.crop[3];
-    if (x0 == 0 && y0 == 0 && x1 == 0 && y1 == 0) { x1 = rp.width; y1 = rp.height; }
-    if (x1 > rp.width || y1 > rp.height || x0 >= x1 || y0 >= y1)
-        return set_error(ctx, PYRE_ERR_INVALID, "crop outside the image");
     if (camera->kind > PYRE_CAMERA_THIN_LENS) return set_error(ctx, PYRE_ERR_INVALID, "unknown camera kind");
 
     WaveParams W;
     std::memset(&W, 0, sizeof W);
     W.cam = make_camera(*camera);
     W.width = rp.width; W.height = rp.height;
-    W.cx0 = x0; W.cy0 = y0; W.cw = x1 - x0; W.ch = y1 - y0;
-    W.npix = W.cw * W.ch;
+    W.cx0 = c[0]; W.cy0 = c[1]; W.cw = c[2] - c[0]; W.ch = c[3] - c[1];
+    W.npix = npix;
     W.spp_begin = rp.spp_begin; W.spp_end = rp.spp_end;
     W.max_depth = rp.max_depth; W.min_rr = rp.min_rr_depth;
     W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);
@@ -1500,7 +1518,7 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     W.refill_any = refill_lanes(&rp, true);
     W.sort = rp.sort_by_material ? 1 : 0;
     DevScene D;
-    int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width, false);
+    rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width, false);
     if (rc) return rc;
     const uint32_t ns = std::max(W.ns, 1u);
     const size_t cap = PYRE_NOALLOC_SCRATCH_BYTES;
@@ -1519,7 +1537,14 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     const uint32_t spp = rp.spp_end - rp.spp_begin;
     uint64_t target = rp.wave_paths ? rp.wave_paths : (uint64_t)8 << 20;
     uint64_t K = std::min<uint64_t>(std::max<uint64_t>(1, target / W.npix), spp);
-    while (K > 1 && carve_paths(nullptr, (size_t)W.npix * K, ns, W.npix, nullptr) > cap) --K;
+    if (carve_paths(nullptr, (size_t)W.npix * K, ns, W.npix, nullptr) > cap) {
+        uint64_t lo = 1, hi = K - 1;  // largest K whose wave fits (K = 1 fits, checked above)
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi + 1) / 2;
+            if (carve_paths(nullptr, (size_t)W.npix * mid, ns, W.npix, nullptr) <= cap) lo = mid; else hi = mid - 1;
+        }
+        K = lo;
+    }
     W.k_per_wave = (uint32_t)K;
     const uint32_t waves = (uint32_t)((spp + K - 1) / K);
 
@@ -1529,7 +1554,7 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     PathSoA S;
     carve_paths((char*)scratch, (size_t)W.npix * K, ns, W.npix, &S);
 
-    const Launch Lc = make_launch<false>(ctx, 0u, W.bvh_width);
+    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
 
     cudaStream_t st = ctx->stream;
     // The array keeps the previous call's contents: clear the sums and counters.
@@ -1678,16 +1703,17 @@ std::string tape_key(const pyre_scene* scene, const pyre_camera_desc* camera, co
     k.append(reinterpret_cast<const char*>(f), sizeof f);
     return k;
 }
-uint64_t crop_pixels(const pyre_render_params& rp) {
-    uint32_t x0 = rp.crop[0], y0 = rp.crop[1], x1 = rp.crop[2], y1 = rp.crop[3];
-    if (x0 == 0 && y0 == 0 && x1 == 0 && y1 == 0) { x1 = rp.width; y1 = rp.height; }
-    return (x1 > x0 && y1 > y0) ? (uint64_t)(x1 - x0) * (y1 - y0) : 0;
-}
 int forward_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera_desc* camera,
                  const pyre_render_params* params, pyre_film* film) {
     const pyre_render_params& rp = *params;
-    const uint64_t paths = crop_pixels(rp) * (rp.spp_end > rp.spp_begin ? rp.spp_end - rp.spp_begin : 0);
-    int rc = ensure_workspace(ctx, ctx->tape_ws, std::max<uint64_t>(paths, 1) * sizeof(float4));
+    uint32_t c[4], npix = 0;
+    int rc = resolve_crop(ctx, rp, "pyre_forward", c, &npix);
+    if (rc) return rc;
+    if (rp.spp_end <= rp.spp_begin) return set_error(ctx, PYRE_ERR_INVALID, "empty sample range");
+    const uint64_t paths = (uint64_t)npix * (rp.spp_end - rp.spp_begin);
+    if (paths > ((uint64_t)1 << 40))
+        return set_error(ctx, PYRE_ERR_INVALID, "pyre_forward: more than 2^40 paths to keep for the adjoint");
+    rc = ensure_workspace(ctx, ctx->tape_ws, std::max<uint64_t>(paths, 1) * sizeof(float4));
     if (rc) return rc;
     ctx->tape_key.clear();
     rc = render_impl(ctx, scene, camera, params, film, (float4*)ctx->tape_ws.ptr);
@@ -1712,7 +1738,9 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_backward: NULL argument");
     PYRE_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     const pyre_render_params& rp = *params;
-    if (rp.width == 0 || rp.height == 0) return set_error(ctx, PYRE_ERR_INVALID, "image size is zero");
+    uint32_t c[4], npix = 0;
+    int rc = resolve_crop(ctx, rp, "pyre_backward", c, &npix);
+    if (rc) return rc;
     if (rp.spp_end <= rp.spp_begin) return set_error(ctx, PYRE_ERR_INVALID, "empty sample range");
     if (rp.max_depth > PYRE_MAX_DEPTH) return set_error(ctx, PYRE_ERR_INVALID, "max_depth above 64");
     if (scene->n_parts != 1) return set_error(ctx, PYRE_ERR_UNSUPPORTED, "pyre_backward: batched scenes");
@@ -1721,11 +1749,6 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_backward: bad image_mem");
     if (grads->mem != PYRE_MEM_HOST && grads->mem != PYRE_MEM_DEVICE)
         return set_error(ctx, PYRE_ERR_INVALID, "pyre_backward: bad grads.mem");
-    uint32_t x0 = rp.crop[0], y0 = rp.crop[1], x1 = rp.crop[2], y1 = rp.crop[3];
-    if (x0 == 0 && y0 == 0 && x1 == 0 && y1 == 0) { x1 = rp.width; y1 = rp.height; }
-    if (x1 > rp.width || y1 > rp.height || x0 >= x1 || y0 >= y1)
-        return set_error(ctx, PYRE_ERR_INVALID, "crop outside the image");
-    int rc;
     // L_total of every path: kept by pyre_forward with the same arguments, or recomputed now
     if (ctx->tape_key != tape_key(scene, camera, rp)) {
         pyre_film none;
@@ -1738,8 +1761,8 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     std::memset(&W, 0, sizeof W);
     W.cam = make_camera(*camera);
     W.width = rp.width; W.height = rp.height;
-    W.cx0 = x0; W.cy0 = y0; W.cw = x1 - x0; W.ch = y1 - y0;
-    W.npix = W.cw * W.ch;
+    W.cx0 = c[0]; W.cy0 = c[1]; W.cw = c[2] - c[0]; W.ch = c[3] - c[1];
+    W.npix = npix;
     W.spp_begin = rp.spp_begin; W.spp_end = rp.spp_end;
     W.max_depth = rp.max_depth; W.min_rr = rp.min_rr_depth;
     W.ns = scene->dev.n_lights + (scene->dev.has_env ? 1u : 0u);

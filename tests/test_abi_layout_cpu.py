@@ -90,10 +90,11 @@ def _c_struct_fields(header: str) -> dict:
 
 
 def test_rust_binding_sketch_matches_the_header():
-    """The #[repr(C)] structs of the Rust binding in INTEGRATION.md list the
-    C structs' fields in the same order (no Rust compiler checks them here)."""
+    """The #[repr(C)] structs of the Rust binding (include/pyre_cuda_ffi.rs)
+    list the C structs' fields in the same order (no Rust compiler checks them
+    here)."""
     import re
-    doc = (ROOT / "INTEGRATION.md").read_text()
+    doc = (ROOT / "include" / "pyre_cuda_ffi.rs").read_text()
     cs = _c_struct_fields((ROOT / "include" / "pyre_cuda.h").read_text())
     rust = {m.group(1): re.findall(r"pub (\w+):", m.group(2))
             for m in re.finditer(r"#\[repr\(C\)\] pub struct (\w+) \{(.*?)\}", doc, re.S)}

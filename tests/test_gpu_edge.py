@@ -97,3 +97,49 @@ def test_invalid_parameters_are_rejected(gpu_ctx, kw, match):
     args.update(kw)
     with pytest.raises(PyreError, match=match):
         gpu_ctx.render(ds, cam, args["integrator"], args["width"], args["height"], args["spp"], crop=args["crop"])
+
+
+def test_crop_area_above_2_31_is_rejected_before_any_work(gpu_ctx):
+    """A 65536 x 65536 crop has 2^32 pixels, which wraps a 32-bit product to 0: every entry point must reject
+    it from the 64-bit pixel count with PYRE_ERR_INVALID (the buffers passed are tiny: nothing may be written)."""
+    import ctypes as C
+
+    from pyre_gb300 import native as N
+    from pyre_gb300.scene import CudaIntegrator
+    sc, cam = P.cornell_box(), P.cornell_box_camera(65536, 65536)
+    ds = gpu_ctx.upload(sc)
+    lib, h = gpu_ctx.lib, gpu_ctx.handle
+    desc = cam.to_desc()
+    params = CudaIntegrator.params(65536, 65536, 0, 1, PathIntegrator(8, 3))
+    buf = np.zeros(16, np.float32)
+    hfilm = N.Film(N.fptr(buf), None, None, None, N.PYRE_MEM_HOST)
+    calls = {
+        "pyre_render": lambda: lib.pyre_render(h, ds.handle, C.byref(desc), C.byref(params), C.byref(hfilm)),
+        "pyre_forward": lambda: lib.pyre_forward(h, ds.handle, C.byref(desc), C.byref(params), C.byref(hfilm)),
+        "pyre_render_progressive": lambda: lib.pyre_render_progressive(h, ds.handle, C.byref(desc), C.byref(params),
+                                                                       N.fptr(buf), N.PYRE_MEM_HOST),
+        "pyre_backward": lambda: lib.pyre_backward(
+            h, ds.handle, C.byref(desc), C.byref(params), N.fptr(buf), N.PYRE_MEM_HOST,
+            C.byref(N.Gradients(None, None, N.PYRE_MEM_HOST))),
+    }
+    import torch
+    dbuf = torch.zeros(16, dtype=torch.float32, device="cuda")
+    dfilm = N.Film(N.dptr(dbuf), None, None, None, N.PYRE_MEM_DEVICE)
+    calls["pyre_render_noalloc"] = lambda: lib.pyre_render_noalloc(h, ds.handle, C.byref(desc), C.byref(params),
+                                                                   C.byref(dfilm))
+    for name, call in calls.items():
+        assert call() == N.PYRE_ERR_INVALID, name
+        assert b"2^31" in lib.pyre_last_error(h), (name, lib.pyre_last_error(h))
+    # the same crop as a batch job
+    db = gpu_ctx.upload_batch([sc])
+    job = N.BatchJob()
+    job.part, job.camera, job.width, job.height = 0, desc, 65536, 65536
+    job.spp_begin, job.spp_end, job.max_depth, job.min_rr_depth = 0, 1, 8, 3
+    job.film = hfilm
+    assert lib.pyre_render_batch(h, db.handle, C.byref(job), 1, C.byref(params)) == N.PYRE_ERR_INVALID
+    assert b"2^31" in lib.pyre_last_error(h)
+    # the context is still usable
+    film = gpu_ctx.render(ds, P.cornell_box_camera(8, 8), PathIntegrator(8, 3), 8, 8, 1)
+    assert np.isfinite(film.radiance).all()
+    db.close()
+    ds.close()

@@ -57,8 +57,33 @@ def test_noalloc_matches_render_twice(gpu_ctx, name):
         assert _relmse(rad, ref.radiance) < 1e-2
         np.testing.assert_allclose(rad, ref.radiance, rtol=1e-6, atol=1e-7)
         np.testing.assert_allclose(out["albedo"].reshape(ref.albedo.shape), ref.albedo, rtol=1e-6, atol=1e-7)
+        np.testing.assert_allclose(out["normal"].reshape(ref.normal.shape), ref.normal, rtol=1e-6, atol=1e-7)
         np.testing.assert_allclose(out["depth"].reshape(ref.depth.shape), ref.depth, rtol=1e-6, atol=1e-7)
     ds.close()
+
+
+def test_noalloc_on_fresh_context_allocates_nothing(gpu_ctx):
+    """A context that has never rendered: every allocation it would try from now on fails (injected
+    out-of-memory), yet pyre_render_noalloc succeeds, twice, with the same film as pyre_render."""
+    sc, cam, w, h = P.cornell_box(), P.cornell_box_camera(96, 96), 96, 96
+    it = PathIntegrator(8, 3)
+    ref = gpu_ctx.render(gpu_ctx.upload(sc), cam, it, w, h, 4)
+    fresh = CudaIntegrator(0)
+    try:
+        ds = fresh.upload(sc)
+        params = CudaIntegrator.params(w, h, 0, 4, it)
+        fresh.check(fresh.lib.pyre_inject_alloc_failure(fresh.handle, 0))
+        try:
+            for _ in range(2):
+                out = _noalloc(fresh, ds, cam, params, w * h)
+                np.testing.assert_allclose(out["radiance"].reshape(ref.radiance.shape), ref.radiance,
+                                           rtol=1e-6, atol=1e-7)
+                np.testing.assert_allclose(out["normal"].reshape(ref.normal.shape), ref.normal, rtol=1e-6, atol=1e-7)
+        finally:
+            fresh.check(fresh.lib.pyre_inject_alloc_failure(fresh.handle, -1))
+        ds.close()
+    finally:
+        fresh.close()
 
 
 def test_noalloc_rejects_oversized_crop(gpu_ctx):
