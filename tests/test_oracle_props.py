@@ -1,7 +1,8 @@
 """Self-checks of the oracle that need no reference output.
 
-* Xoshiro256++ / SplitMix64 follow the published algorithm (first output of a
-  hand-set state derived by hand; stream statistics uniform);
+* Xoshiro256++ / SplitMix64 follow the published algorithms: outputs worked
+  out by hand, and 10^6 words per seed equal to an independent C restatement
+  (tests/native/xoshiro_published.c); stream statistics uniform;
 * BVH traversal equals brute force over all triangles;
 * the reference's visit-order tie rule and the canonical rule agree;
 * environment sampling returns the pdf that pdf(wi) evaluates;
@@ -25,21 +26,72 @@ def test_rng_stream_statistics(oracle_mod):
     assert abs(np.corrcoef(u[:-1], u[1:])[0, 1]) < 0.01
 
 
-def test_splitmix_seeding_first_output(oracle_mod):
-    """seed_from_u64(0): state word 0 = SplitMix64 of 0x9E3779B97F4A7C15 (computed here in Python)."""
+@pytest.fixture(scope="module")
+def published_rng(tmp_path_factory):
+    """tests/native/xoshiro_published.c (SplitMix64, xoshiro256++, rand_xoshiro's seeding and rand's f32
+    mapping, written from the published algorithms) compiled with gcc."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    from pathlib import Path
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    so = tmp_path_factory.mktemp("pubrng") / "libxoshiro_published.so"
+    src = Path(__file__).parent / "native" / "xoshiro_published.c"
+    r = subprocess.run([cc, "-O2", "-shared", "-fPIC", "-ffp-contract=off", str(src), "-o", str(so)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lib = C.CDLL(str(so))
+    u64p, f32p = C.POINTER(C.c_uint64), C.POINTER(C.c_float)
+    lib.pub_u64_stream.argtypes = [C.c_uint64, C.c_uint32, u64p]
+    lib.pub_f32_stream.argtypes = [C.c_uint64, C.c_uint32, f32p]
+    lib.pub_u64_from_state.argtypes = [u64p, C.c_uint32, u64p]
+    lib.pub_splitmix_stream.argtypes = [C.c_uint64, C.c_uint32, u64p]
+    return lib
+
+
+def _u64(lib_fn, *args, n):
+    import ctypes as C
+    out = np.zeros(n, np.uint64)
+    lib_fn(*args, n, out.ctypes.data_as(C.POINTER(C.c_uint64)))
+    return out
+
+
+def test_published_xoshiro_hand_derived_outputs(published_rng):
+    """From the state (1, 2, 3, 4): the first output is rotl(1 + 4, 23) + 1 = 41943041. One update gives the
+    state (7, 0, 262146, 6 * 2^45), so the second output is rotl(7 + 6 * 2^45, 23) + 7 = 7 * 2^23 + 96 + 7
+    = 58720359 (6 * 2^68 wraps to 0 and 6 * 2^45 >> 41 = 96). SplitMix64 from x = 0 first mixes
+    z = 0x9e3779b97f4a7c15; both are worked out by hand here, independent of either implementation."""
+    import ctypes as C
+    st = np.array([1, 2, 3, 4], np.uint64)
+    out = _u64(published_rng.pub_u64_from_state, st.ctypes.data_as(C.POINTER(C.c_uint64)), n=2)
+    assert [int(v) for v in out] == [41943041, 58720359]
     m = (1 << 64) - 1
+    z = 0x9E3779B97F4A7C15
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+    assert int(_u64(published_rng.pub_splitmix_stream, 0, n=1)[0]) == z ^ (z >> 31)
 
-    def mix(z):
-        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
-        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
-        return z ^ (z >> 31)
 
-    state = [mix((0x9E3779B97F4A7C15 * (k + 1)) & m) for k in range(4)]
-    s0, s1, s2, s3 = state
-    first = ((((s0 + s3) & m) << 23 | ((s0 + s3) & m) >> 41) & m)
-    first = (first + s0) & m
-    out = oracle_mod.rng_u64_stream(0, 1)
-    assert int(out[0]) == first
+@pytest.mark.parametrize("seed", [0, 1, 12345, (1 << 64) - 1, 0x9E3779B97F4A7C15, "pixel"])
+def test_oracle_sampler_equals_published_generators(oracle_mod, published_rng, seed):
+    """The oracle's IndependentSampler (sampler.rs:15-36) against the independent restatement: the first 10^6
+    next_u64 outputs after seed_from_u64 are equal word for word, and the f32 draws equal rand's
+    (next_u32 >> 8) * 2^-24 with next_u32 = next_u64 >> 32, on the same stream."""
+    import ctypes as C
+    if seed == "pixel":
+        seed = oracle_mod.pixel_seed(1919, 1079, 63)
+    n = 1_000_000
+    assert np.array_equal(oracle_mod.rng_u64_stream(seed, n), _u64(published_rng.pub_u64_stream, seed, n=n))
+    f_pub = np.zeros(n, np.float32)
+    published_rng.pub_f32_stream(seed, n, f_pub.ctypes.data_as(C.POINTER(C.c_float)))
+    f_orc, _ = oracle_mod.rng_stream(seed, n)
+    assert np.array_equal(f_orc.view(np.uint32), f_pub.view(np.uint32))
+    # the mapping itself, from the u64 words
+    words = _u64(published_rng.pub_u64_stream, seed, n=n)
+    mapped = ((words >> np.uint64(40)).astype(np.float64) * 2.0 ** -24).astype(np.float32)
+    assert np.array_equal(mapped, f_orc)
 
 
 def test_traversal_equals_brute_force(oracle_mod):
