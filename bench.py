@@ -263,10 +263,30 @@ def make_workload():
     return scene, cam, time.time() - t0
 
 
+def cpu_model() -> str:
+    """CPU model name of this host (lscpu, else /proc/cpuinfo, else the platform string)."""
+    import platform
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
+
+
 def cpu_sample(scene, cam, rows: int, threads: int):
-    """Oracle render of `rows` image rows spread over the frame at full spp."""
+    """Oracle render of `rows` image rows spread over the frame at full spp, with the oracle built for this CPU
+    (-mcpu=native / -march=native, no FMA contraction: the same bits as the portable build)."""
     from oracle import oracle as O
-    osc = O.OracleScene(scene, nthreads=threads)
+    osc = O.OracleScene(scene, nthreads=threads, build="native")
     ys = np.linspace(0, H - 1, rows).round().astype(int)
     t0 = time.time()
     for y in ys:
@@ -276,15 +296,26 @@ def cpu_sample(scene, cam, rows: int, threads: int):
     return samples / dt / 1e6, dt, samples
 
 
+def cpu_build_info(scene, cam, threads: int) -> dict:
+    """Flags and CPU of the timed oracle build, and whether it renders the portable build's bits (a 64x2 crop)."""
+    from oracle import oracle as O
+    crop = (W // 2 - 32, H // 2 - 1, W // 2 + 32, H // 2 + 1)
+    a = O.OracleScene(scene, nthreads=threads).render(cam, W, H, 4, crop=crop)["radiance"]
+    b = O.OracleScene(scene, nthreads=threads, build="native").render(cam, W, H, 4, crop=crop)["radiance"]
+    return {"flags": O.native_flags(), "cpu_model": cpu_model(),
+            "bit_identical_to_portable_build": bool(np.array_equal(a.view(np.uint32), b.view(np.uint32)))}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     from oracle import oracle as O
-    O.lib()
+    O.lib("native")
     scene, cam, _ = make_workload()
     threads = os.cpu_count() or 1
     rows = args.cpu_rows or CPU_ROWS
+    binfo = cpu_build_info(scene, cam, threads)
     for _ in range(args.warmup):
         cpu_sample(scene, cam, max(1, rows // 4), threads)
     vals, times = [], []
@@ -302,7 +333,7 @@ def run_reference(args):
                        "parallelism": "cpu threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample + "; C++ restatement of the reference's CPU path (the Rust "
-                                       "reference cannot be built here)"},
+                                       "reference cannot be built here)", **binfo},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -449,11 +480,12 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rows = args.cpu_rows or CPU_ROWS
+        binfo = cpu_build_info(scene, cam, threads)
         v, dt, n = cpu_sample(scene, cam, rows, threads)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{rows} rows x 1920 px at 64 spp ({n} samples, {dt:.1f} s); C++ "
                                           "restatement of the reference's CPU path (Rust reference not buildable "
-                                          "here)"}
+                                          "here)", **binfo}
     line["clocks"] = clk.summary()
     if rank == 0:
         print(json.dumps(line), flush=True)

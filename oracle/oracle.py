@@ -17,6 +17,9 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "libpyre_oracle.so"
+# the same source built for the CPU it runs on (-mcpu=native / -march=native):
+# the timed CPU baseline of bench.py; results are bit-identical to LIB's
+LIB_NATIVE = HERE / "_build" / "libpyre_oracle_native.so"
 F32 = np.float32
 
 P_f = C.POINTER(C.c_float)
@@ -63,28 +66,35 @@ _SIG = {
                                C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, P_f, P_d, C.c_int]),
 }
 
-_lib = None
+_libs: dict = {}
 
 
 def build() -> Path:
-    """Compiles the oracle with its Makefile (g++, -ffp-contract=off)."""
+    """Compiles both builds of the oracle with its Makefile (g++, -ffp-contract=off)."""
     r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
-def lib() -> C.CDLL:
-    global _lib
-    if _lib is None:
-        if not LIB.exists() or LIB.stat().st_mtime < (HERE / "pyre_oracle.cpp").stat().st_mtime:
+def native_flags() -> str:
+    """The compiler command line of the CPU-tuned build."""
+    f = HERE / "_build" / "native_flags.txt"
+    return f.read_text().strip() if f.exists() else ""
+
+
+def lib(kind: str = "portable") -> C.CDLL:
+    """The portable build (the checker) or the CPU-tuned one ("native", for timing)."""
+    if kind not in _libs:
+        path = {"portable": LIB, "native": LIB_NATIVE}[kind]
+        if not path.exists() or path.stat().st_mtime < (HERE / "pyre_oracle.cpp").stat().st_mtime:
             build()
-        L = C.CDLL(str(LIB))
+        L = C.CDLL(str(path))
         for k, (res, args) in _SIG.items():
             fn = getattr(L, k)
             fn.restype, fn.argtypes = res, args
-        _lib = L
-    return _lib
+        _libs[kind] = L
+    return _libs[kind]
 
 
 def _f(a):
@@ -184,9 +194,9 @@ def bvh_build(mesh):
 class OracleScene:
     """The reference's Scene (scene.rs:24-34) built from a pyre_gb300.scene.Scene."""
 
-    def __init__(self, scene, nthreads: int = 0):
+    def __init__(self, scene, nthreads: int = 0, build: str = "portable"):
         from pyre_gb300.scene import DisneyBsdf, Lambertian
-        L = lib()
+        L = self.L = lib(build)
         self.h = C.c_void_p(L.orc_scene_new())
         self.nthreads = nthreads
         for m in scene.materials:
@@ -227,15 +237,15 @@ class OracleScene:
 
     def __del__(self):
         try:
-            lib().orc_scene_free(self.h)
+            self.L.orc_scene_free(self.h)
         except Exception:
             pass
 
     def bvh(self, prim: int):
         from pyre_gb300.native import BVH2_DTYPE
-        n = lib().orc_scene_bvh_nodes(self.h, prim, None, None)
+        n = self.L.orc_scene_bvh_nodes(self.h, prim, None, None)
         nodes = np.zeros(n, BVH2_DTYPE)
-        lib().orc_scene_bvh_nodes(self.h, prim, nodes.ctypes.data_as(C.c_void_p), None)
+        self.L.orc_scene_bvh_nodes(self.h, prim, nodes.ctypes.data_as(C.c_void_p), None)
         return nodes
 
     def intersect(self, org, dirs, tmin, tmax, time=None, canonical=True, normals=False):
@@ -246,7 +256,7 @@ class OracleScene:
         out.update({k: np.zeros(n, F32) for k in ("t", "u", "v")})
         if normals:
             out["normal"] = np.zeros((n, 3), F32)
-        lib().orc_intersect(self.h, _f(org), _f(dirs), _f(tmin), _f(tmax), _f(t_), n, 1 if canonical else 0,
+        self.L.orc_intersect(self.h, _f(org), _f(dirs), _f(tmin), _f(tmax), _f(t_), n, 1 if canonical else 0,
                             self.nthreads, out["kind"].ctypes.data_as(P_i32), out["instance"].ctypes.data_as(P_i32),
                             out["triangle"].ctypes.data_as(P_i32), _f(out["t"]), _f(out["u"]), _f(out["v"]),
                             _f(out.get("normal")))
@@ -257,7 +267,7 @@ class OracleScene:
         n = tmin.size
         t_ = _c(time) if time is not None else None
         occ = np.zeros(n, np.uint8)
-        lib().orc_occluded(self.h, _f(org), _f(dirs), _f(tmin), _f(tmax), _f(t_), n, self.nthreads,
+        self.L.orc_occluded(self.h, _f(org), _f(dirs), _f(tmin), _f(tmax), _f(t_), n, self.nthreads,
                            occ.ctypes.data_as(P_u8))
         return occ
 
@@ -266,7 +276,7 @@ class OracleScene:
         n = q.shape[0]
         wi, li, pdf = np.zeros((n, 3), F32), np.zeros((n, 3), F32), np.zeros(n, F32)
         pdf_back, le_back = np.zeros(n, F32), np.zeros((n, 3), F32)
-        lib().orc_env_query(self.h, _f(q), n, _f(wi), _f(li), _f(pdf), _f(pdf_back), _f(le_back))
+        self.L.orc_env_query(self.h, _f(q), n, _f(wi), _f(li), _f(pdf), _f(pdf_back), _f(le_back))
         return wi, li, pdf, pdf_back, le_back
 
     def render(self, camera, width, height, spp, spp_begin=0, crop=None, max_depth=8, min_rr_depth=3,
@@ -278,7 +288,7 @@ class OracleScene:
         rgb, alb, nor, dep = (np.zeros((ch, cw, 3), F32), np.zeros((ch, cw, 3), F32), np.zeros((ch, cw, 3), F32),
                               np.zeros((ch, cw), F32))
         acc = np.zeros((ch, cw, 3), np.float64) if accum64 else None
-        b = lib().orc_render(self.h, _f(cam), width, height, spp_begin, spp_begin + spp, max_depth, min_rr_depth,
+        b = self.L.orc_render(self.h, _f(cam), width, height, spp_begin, spp_begin + spp, max_depth, min_rr_depth,
                              x0, y0, x1, y1, self.nthreads, _f(rgb), _f(alb), _f(nor), _f(dep),
                              acc.ctypes.data_as(P_d) if acc is not None else None)
         return {"radiance": rgb, "albedo": alb, "normal": nor, "depth": dep, "bounces": int(b), "accum64": acc}
@@ -291,7 +301,7 @@ class OracleScene:
         d = _c(dl_di).reshape(-1)
         n_env = 0 if env_shape is None else env_shape[0] * env_shape[1] * 3
         out = np.zeros(n_materials * 6 + n_env, np.float64)
-        lib().orc_render_grad(self.h, _f(camera.as_array()), width, height, spp_begin, spp_begin + spp, max_depth,
+        self.L.orc_render_grad(self.h, _f(camera.as_array()), width, height, spp_begin, spp_begin + spp, max_depth,
                               min_rr_depth, x0, y0, x1, y1, _f(d), out.ctypes.data_as(P_d), self.nthreads)
         mat = out[: n_materials * 6].reshape(n_materials, 6)
         env = out[n_materials * 6:].reshape(env_shape[0], env_shape[1], 3) if env_shape is not None else None
@@ -299,7 +309,7 @@ class OracleScene:
 
     def render_one(self, camera, width, height, x, y, s, max_depth=8, min_rr_depth=3):
         out = np.zeros(10, F32)
-        lib().orc_render_one(self.h, _f(camera.as_array()), width, height, x, y, s, max_depth, min_rr_depth, _f(out))
+        self.L.orc_render_one(self.h, _f(camera.as_array()), width, height, x, y, s, max_depth, min_rr_depth, _f(out))
         return out
 
 

@@ -24,6 +24,9 @@ def test_reference_arm_prints_the_contract_line():
     cb = line["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == line["value"]
     assert cb["unit"] == line["unit"] and cb["sample"]
+    # the timed build is the CPU-tuned one, with its flags and the CPU model stated
+    assert "native" in cb["flags"] and cb["cpu_model"]
+    assert cb["bit_identical_to_portable_build"] is True
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
