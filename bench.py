@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--workload", default="studio", choices=["studio", "batch", "adjoint"],
                     help="studio: the 1080p headline frame; batch: 256 Cornell-variant jobs in one batched launch")
     ap.add_argument("--jobs", type=int, default=256, help="batch workload: number of jobs")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the microbenchmark, adjoint and batch entries of the studio line")
     return ap.parse_args()
 
 
@@ -206,6 +208,182 @@ def run_batch(args):
     ds.close()
     ctx.close()
     return 0
+
+
+def extra_microbench(reps: int = 3) -> dict:
+    """The ray-intersection microbenchmark: level-8 displaced icosphere (1,310,720 triangles), 16,777,216 rays
+    from seed 1, closest hit and any hit. Device rate: rays and hits resident in HBM, the query kernel's CUDA-event
+    time. End to end: the same call with host rays and host results (copies inside the timed region)."""
+    import ctypes as C
+
+    import torch
+
+    from pyre_gb300 import CudaIntegrator
+    from pyre_gb300 import native as N
+    from pyre_gb300 import presets as P
+    sc = P.microbench_scene(level=8)
+    mesh = sc.primitives[0].instance.mesh
+    n = 1 << 24
+    org, d, tmin, tmax = P.random_rays(mesh, n, seed=1)
+    ctx = CudaIntegrator(0)
+    ctx.set_bvh_builder("device")  # the same BVH as the host build, built in ~30 ms
+    ds = ctx.upload(sc)
+    dev = {k: torch.from_numpy(v).cuda() for k, v in (("o", org), ("d", d), ("tmin", tmin), ("tmax", tmax))}
+    rays = N.Rays(N.dptr(dev["o"]), N.dptr(dev["d"]), N.dptr(dev["tmin"]), N.dptr(dev["tmax"]), None)
+    out = {k: torch.empty(n, dtype=torch.int32, device="cuda") for k in ("kind", "inst", "tri")}
+    out.update({k: torch.empty(n, dtype=torch.float32, device="cuda") for k in ("t", "u", "v")})
+    occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    hits = N.Hits(N.dptr(out["kind"], C.c_int32), N.dptr(out["inst"], C.c_int32), N.dptr(out["tri"], C.c_int32),
+                  N.dptr(out["t"]), N.dptr(out["u"]), N.dptr(out["v"]))
+    res = {"workload": "displaced icosphere level 8 (1,310,720 triangles), 16,777,216 rays from seed 1, "
+                       "t_min 1e-4, t_max inf", "rays": n, "triangles": int(mesh.triangle_count())}
+    for q in ("closest", "any"):
+        def call():
+            if q == "closest":
+                ctx.check(ctx.lib.pyre_intersect_closest(ctx.handle, ds.handle, C.byref(rays), n, C.byref(hits),
+                                                         N.PYRE_MEM_DEVICE))
+            else:
+                ctx.check(ctx.lib.pyre_intersect_any(ctx.handle, ds.handle, C.byref(rays), n,
+                                                     N.dptr(occ, C.c_uint8), N.PYRE_MEM_DEVICE))
+            return ctx.stats().ms_total
+        call()
+        ms = sorted(call() for _ in range(reps))[reps // 2]
+        res[f"{q}_grays_per_s"] = n / ms / 1e6
+        res[f"{q}_ms"] = ms
+        # end to end through the Python API: host arrays in and out
+        ctx.intersect(ds, org, d, tmin, tmax, any_hit=(q == "any"))
+        t0 = time.perf_counter()
+        ctx.intersect(ds, org, d, tmin, tmax, any_hit=(q == "any"))
+        res[f"{q}_e2e_grays_per_s"] = n / (time.perf_counter() - t0) / 1e9
+    res["gpu_launches"] = 2 * reps
+    ds.close()
+    ctx.close()
+    return res
+
+
+def extra_adjoint(reps: int = 3) -> dict:
+    """The differentiable render: the studio at 512x512 (64 sphere materials + ground, 512x256 HDRI), 32 spp
+    forward (pyre_forward) + 32 spp path-replay adjoint (pyre_backward) of an L2 loss against a target rendered
+    from perturbed parameters. Device times from the library's CUDA events."""
+    from pyre_gb300 import CudaIntegrator, PathIntegrator
+    from pyre_gb300 import presets as P
+    w = h = 512
+    spp = 32
+    sc, tgt, cam = P.adjoint_problem(w, h)
+    ctx = CudaIntegrator(0)
+    ds, dt = ctx.upload(sc), ctx.upload(tgt)
+    it = PathIntegrator(8, 3)
+    target = ctx.render(dt, cam, it, w, h, 64, spp_begin=1 << 20).radiance.astype(np.float64)
+    fwd, adj, wall = [], [], []
+    for k in range(reps + 1):
+        t0 = time.perf_counter()
+        img = ctx.forward(ds, cam, it, w, h, spp, spp_begin=k * spp).radiance
+        f_ms = ctx.stats().ms_total
+        dl = (2.0 * (img - target) / img.size).astype(np.float32)
+        ctx.backward(ds, cam, it, w, h, spp, dl, spp_begin=k * spp)
+        if k:
+            fwd.append(f_ms)
+            adj.append(ctx.stats().ms_total)
+            wall.append(time.perf_counter() - t0)
+    f, a = float(np.median(fwd)), float(np.median(adj))
+    ds.close()
+    dt.close()
+    ctx.close()
+    return {"workload": "studio 512x512, 65 materials, 512x256 HDRI, 32 spp forward + 32 spp adjoint, depth 8",
+            "parameters": len(sc.materials) * 6 + sc.env.width * sc.env.height * 3,
+            "forward_ms": f, "adjoint_ms": a, "forward_plus_adjoint_over_forward": (f + a) / f,
+            "e2e_step_ms": 1e3 * float(np.median(wall))}
+
+
+def extra_batch(reps: int = 1) -> dict:
+    """256 batched jobs (Cornell variants with 10..200k-triangle inserts, 128^2..1024^2, 4/16/64 spp, depth
+    4-12) against one pyre_render per job. Both arms write host films and are timed on the wall clock (e2e:
+    every launch, host gap, film copy and synchronisation) and by the library's CUDA events (device)."""
+    from pyre_gb300 import CudaIntegrator
+    from pyre_gb300 import presets as P
+    jobs = P.batch_jobs(256, seed=11)
+    spec = [{"part": k, "camera": j["camera"], "width": j["width"], "height": j["height"], "spp": j["spp"],
+             "integrator": j["integrator"]} for k, j in enumerate(jobs)]
+    samples = sum(j["width"] * j["height"] * j["spp"] for j in jobs)
+    ctx = CudaIntegrator(0)
+    ctx.set_bvh_builder("device")
+    ds = ctx.upload_batch([j["scene"] for j in jobs])
+    singles = [ctx.upload(j["scene"]) for j in jobs]
+
+    def batched():
+        t0 = time.perf_counter()
+        ctx.render_batch(ds, spec, use_graph=1)
+        return time.perf_counter() - t0, ctx.stats().ms_total / 1e3
+
+    def per_view(small_only=False):
+        wall = dev = 0.0
+        n = 0
+        for ds1, j in zip(singles, jobs):
+            if small_only and j["width"] > 256:
+                continue
+            t0 = time.perf_counter()
+            ctx.render(ds1, j["camera"], j["integrator"], j["width"], j["height"], j["spp"])
+            wall += time.perf_counter() - t0
+            dev += ctx.stats().ms_total / 1e3
+            n += j["width"] * j["height"] * j["spp"]
+        return wall, dev, n
+
+    batched()
+    b = sorted(batched() for _ in range(reps))[reps // 2]
+    per_view()
+    v = sorted(per_view()[:2] for _ in range(reps))[reps // 2]
+    # the small views alone (128^2 and 256^2), where launch and host gaps weigh most
+    small_idx = [k for k, j in enumerate(jobs) if j["width"] <= 256]
+    sub = CudaIntegrator(0)
+    sub.set_bvh_builder("device")
+    dsub = sub.upload_batch([jobs[k]["scene"] for k in small_idx])
+    sspec = [dict(spec[k], part=i) for i, k in enumerate(small_idx)]
+    sub.render_batch(dsub, sspec, use_graph=1)
+    t0 = time.perf_counter()
+    sub.render_batch(dsub, sspec, use_graph=1)
+    sb_wall, sb_dev = time.perf_counter() - t0, sub.stats().ms_total / 1e3
+    sv_wall, sv_dev, s_samples = per_view(small_only=True)
+    dsub.close()
+    sub.close()
+    for s1 in singles:
+        s1.close()
+    ds.close()
+    ctx.close()
+    return {"workload": "256 jobs: Cornell variants + 10..200k-triangle displaced spheres, 128^2..1024^2, spp "
+                        "4/16/64, depth 4-12, Disney materials; host films", "samples": samples,
+            "batched_e2e_msamples_per_s": samples / b[0] / 1e6, "batched_device_msamples_per_s": samples / b[1] / 1e6,
+            "per_view_e2e_msamples_per_s": samples / v[0] / 1e6, "per_view_device_msamples_per_s": samples / v[1] / 1e6,
+            "batched_over_per_view_e2e": v[0] / b[0], "batched_over_per_view_device": v[1] / b[1],
+            "small_jobs": {"jobs": len(small_idx), "samples": s_samples,
+                           "batched_over_per_view_e2e": sv_wall / sb_wall,
+                           "batched_over_per_view_device": sv_dev / sb_dev}}
+
+
+def adjoint_cosine_check() -> dict:
+    """Gradient check beside the CPU baseline: pyre_backward on the small gradient-check scene (48x48, 4 spp,
+    depth 6, 4 materials, 16x8 HDRI) against the oracle's forward-mode dual-number gradient (same seeds, same
+    detached convention)."""
+    from oracle import oracle as O
+    from pyre_gb300 import CudaIntegrator, PathIntegrator
+    from pyre_gb300 import native as N
+    from pyre_gb300 import presets as P
+    sc, cam = P.adjoint_check_scene()
+    w = h = 48
+    it = PathIntegrator(6, 3)
+    dl = np.random.default_rng(9).normal(size=(h, w, 3)).astype(np.float32)
+    ctx = CudaIntegrator(0)
+    ds = ctx.upload(sc)
+    g_mat, g_env = ctx.backward(ds, cam, it, w, h, 4, dl, env_sampling=N.PYRE_ENV_CDF)
+    ds.close()
+    ctx.close()
+    o_mat, o_env = O.OracleScene(sc).render_grad(cam, w, h, 4, dl, len(sc.materials), (8, 16), max_depth=6,
+                                                  min_rr_depth=3)
+
+    def cos(a, b):
+        a, b = np.ravel(a).astype(np.float64), np.ravel(b).astype(np.float64)
+        return float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-300))
+    return {"scene": "48x48, 4 spp, depth 6, 4 materials, 16x8 HDRI", "cos_materials": cos(g_mat, o_mat),
+            "cos_env": cos(g_env, o_env)}
 
 
 class Clocks:
@@ -477,7 +655,13 @@ def main():
                     C_sizeof_params(), "d2h_bytes_per_step": npix * 10 * 4},
             "gpu_launches": int(launches),
             "roofline": roofline}
+    if rank == 0 and world == 1 and not args.no_extras:
+        line["microbench"] = extra_microbench()
+        line["adjoint"] = extra_adjoint()
+        line["batch"] = extra_batch()
     if rank == 0 and world == 1 and not args.no_cpu:
+        if "adjoint" in line:
+            line["adjoint"]["gradient_check"] = adjoint_cosine_check()
         threads = os.cpu_count() or 1
         rows = args.cpu_rows or CPU_ROWS
         binfo = cpu_build_info(scene, cam, threads)

@@ -287,7 +287,8 @@ typedef struct pyre_film {
     int mem;         /* PYRE_MEM_HOST or PYRE_MEM_DEVICE */
 } pyre_film;
 
-/* Statistics of the last render on the context. */
+/* Statistics of the last render (or ray query: its rays in extend_rays or
+ * shadow_rays, and the query kernel's device time in ms_total) on the context. */
 typedef struct pyre_render_stats {
     uint64_t samples;         /* paths started */
     uint64_t extend_rays;     /* closest-hit rays traced */

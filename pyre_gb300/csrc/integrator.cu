@@ -1653,9 +1653,11 @@ static int intersect_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_ray
     q.org = org; q.dir = dir; q.tmin = tmin; q.tmax = tmax; q.time = time;
     if (any) q.occluded = occ;
     else { q.kind = kind; q.inst = inst; q.tri = tri; q.tt = tt; q.uu = uu; q.vv = vv; }
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
     if (any) launch_intersect<true>(ctx, D, q, (uint32_t)n, width);
     else launch_intersect<false>(ctx, D, q, (uint32_t)n, width);
     PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[1], st));
     if (mem == PYRE_MEM_HOST) {
         if (any) PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(occluded, occ, n, cudaMemcpyDeviceToHost, st));
         else {
@@ -1668,7 +1670,14 @@ static int intersect_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_ray
         }
     }
     PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-    return take_kernel_error(ctx);
+    if (int rc = take_kernel_error(ctx)) return rc;
+    // statistics: the query kernel's device time and its ray count
+    pyre_render_stats& s = ctx->stats;
+    std::memset(&s, 0, sizeof s);
+    (any ? s.shadow_rays : s.extend_rays) = n;
+    s.kernel_launches = 1;
+    cudaEventElapsedTime(&s.ms_total, ctx->ev[0], ctx->ev[1]);
+    return PYRE_OK;
 }
 
 int pyre_intersect_closest(pyre_ctx* ctx, const pyre_scene* scene, const pyre_rays* rays, uint64_t n, pyre_hits* hits,

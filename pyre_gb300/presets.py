@@ -427,3 +427,21 @@ def adjoint_problem(width: int = 512, height: int = 512, env_size=(512, 256), se
     tgt.env = HdriEnvironmentLight(sc.env.width, sc.env.height, px.astype(F32), sc.env.intensity)
     cam = studio_procedural_camera(width, height)
     return sc, tgt, cam
+
+
+def adjoint_check_scene():
+    """A small scene for gradient checks against the CPU dual-number gradient: a Lambertian ground quad, three
+    Disney spheres (one metallic) and a 16x8 HDRI with one bright texel; 48x48 camera. Returns (scene, camera)."""
+    sc = Scene()
+    sc.materials.append(Lambertian([0.55, 0.5, 0.45]))
+    s = 20.0
+    sc.primitives.append(Primitive(MeshInstance.build(
+        quad_mesh([(-s, 0, -s), (s, 0, -s), (s, 0, s), (-s, 0, s)], (0, 1, 0))), 0))
+    rng = np.random.default_rng(4)
+    for k, (x, z) in enumerate([(-0.5, 0.0), (0.4, 0.1), (0.0, -0.6)]):
+        sc.materials.append(DisneyBsdf(rng.random(3), float(k == 1), 0.2 + 0.3 * k, 0.5))
+        sc.primitives.append(Primitive(MeshInstance.build(make_uv_sphere((x, 0.3, z), 0.3, 24, 12)), k + 1))
+    px = (0.3 + rng.random((8, 16, 3))).astype(F32)
+    px[2, 5] = [20.0, 18.0, 14.0]  # a bright texel
+    sc.env = HdriEnvironmentLight(16, 8, px, 1.0)
+    return sc, studio_ref_camera(48, 48)

@@ -18,20 +18,7 @@ def cosine(a, b):
 
 
 def small_env_scene():
-    sc = Scene()
-    sc.materials.append(Lambertian([0.55, 0.5, 0.45]))
-    s = 20.0
-    sc.primitives.append(Primitive(MeshInstance.build(
-        P.quad_mesh([(-s, 0, -s), (s, 0, -s), (s, 0, s), (-s, 0, s)], (0, 1, 0))), 0))
-    rng = np.random.default_rng(4)
-    for k, (x, z) in enumerate([(-0.5, 0.0), (0.4, 0.1), (0.0, -0.6)]):
-        sc.materials.append(DisneyBsdf(rng.random(3), float(k == 1), 0.2 + 0.3 * k, 0.5))
-        sc.primitives.append(Primitive(MeshInstance.build(P.make_uv_sphere((x, 0.3, z), 0.3, 24, 12)), k + 1))
-    px = (0.3 + rng.random((8, 16, 3))).astype(np.float32)
-    px[2, 5] = [20.0, 18.0, 14.0]  # a bright texel
-    sc.env = HdriEnvironmentLight(16, 8, px, 1.0)
-    cam = P.studio_ref_camera(48, 48)
-    return sc, cam
+    return P.adjoint_check_scene()
 
 
 def test_adjoint_matches_dual_number_oracle(gpu_ctx, oracle_mod):

@@ -2,7 +2,9 @@
 
 At equal spp (16) the GPU and the oracle use the same per-pixel sample seeds,
 so their errors against the high-spp reference must match; at 4096 spp the
-GPU must converge onto the reference (no bias). relMSE = mean over pixels of
+GPU must converge onto the reference (no bias). On the headline scene the
+alias-table environment sampling must be as accurate as CDF inversion: its
+mean error over 32 runs of 1024 spp is within 1.1x of the CDF mode's. relMSE = mean over pixels of
 sum_c (x - r)^2 / (r^2 + 1e-2). Errors are printed (pytest -s) for the record.
 """
 import json
@@ -57,10 +59,21 @@ def test_against_highspp_reference(gpu_ctx, oracle_mod, name):
             if mode == PYRE_ENV_CDF:
                 # same seeds: the two estimates are the same samples
                 assert abs(e16 - e_cpu) <= 0.05 * e_cpu + 1e-6, (e16, e_cpu)
-            else:
-                assert e16 < 3.0 * e_cpu + 1e-4, (e16, e_cpu)
             # convergence: 256x more samples cut the error by well over 16x
             assert e4k < max(e16 / 16.0, 2e-4), (e4k, e16)
+        if name == "studio_procedural":
+            # Alias against CDF sampling of the environment at equal spp: the mean error against the 65,536-spp
+            # reference over 32 disjoint sample ranges of 1024 spp (the same ranges in both modes) is within
+            # 1.1x. Both modes draw the same numbers and trace the same BSDF-sampled paths, so the heavy tail of
+            # this frame's error (caustic paths to the sun) is common to both; the NEE terms differ.
+            errs = {}
+            for mode in (PYRE_ENV_CDF, PYRE_ENV_ALIAS):
+                errs[mode] = float(np.mean([
+                    relmse(gpu_ctx.render(ds, cam, it, w, h, 1024, spp_begin=(1 << 24) + 1024 * r, crop=crop,
+                                          env_sampling=mode).radiance, ref) for r in range(32)]))
+            report[f"{k}/alias_vs_cdf_1024spp_x32"] = {"cdf": errs[PYRE_ENV_CDF], "alias": errs[PYRE_ENV_ALIAS],
+                                                       "ratio": errs[PYRE_ENV_ALIAS] / errs[PYRE_ENV_CDF]}
+            assert errs[PYRE_ENV_ALIAS] <= 1.1 * errs[PYRE_ENV_CDF], report
         k += 1
     assert k > 0
     print(json.dumps({name: report}))

@@ -132,3 +132,25 @@ def test_bvh_width_rejects_bad_values(gpu_ctx):
     for w in (0, 3, 16):
         with pytest.raises(PyreError):
             ds.set_bvh_width(w)
+
+
+def test_microbenchmark_full_size_bit_exact(gpu_ctx, oracle_mod):
+    """The ray-intersection microbenchmark at its own size: the level-8 displaced icosphere (1,310,720
+    triangles, radial value noise of amplitude 0.1) and 16,777,216 rays from seed 1 (origins uniform in the
+    mesh box scaled 1.5x, directions uniform on the sphere). Closest hit: kind, instance, triangle and the bits
+    of t, u and v equal the oracle's (mesh.rs:153-178 on the BVH of bvh.rs:86-153, canonical tie rule); any
+    hit equals Scene::occluded (scene.rs:120-140) for every ray."""
+    sc = P.microbench_scene(level=8)
+    mesh = sc.primitives[0].instance.mesh
+    assert mesh.triangle_count() == 1_310_720
+    org, d, tmin, tmax = P.random_rays(mesh, 16_777_216, seed=1)
+    ds = gpu_ctx.upload(sc)
+    g = gpu_ctx.intersect(ds, org, d, tmin, tmax)
+    osc = oracle_mod.OracleScene(sc)
+    r = osc.intersect(org, d, tmin, tmax, canonical=True)
+    assert 0.2 < (r["kind"] > 0).mean() < 0.5
+    _compare(g, r, "microbenchmark 1.31M triangles x 16.8M rays")
+    del g, r
+    occ = gpu_ctx.intersect(ds, org, d, tmin, tmax, any_hit=True)
+    assert np.array_equal(occ, osc.occluded(org, d, tmin, tmax))
+    ds.close()
