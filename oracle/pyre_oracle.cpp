@@ -1119,7 +1119,7 @@ static void texel_weights(const Env& e, V2 uv, uint32_t idx[4], float wt[4]) {
 }
 
 struct GradPath {
-    size_t n;                    // tangent count
+    size_t n;                    // tangents carried by the throughput: the material parameters
     std::vector<double> beta_d;  // 3 * n: d beta_c / d theta
     std::vector<double>* grad;   // accumulates delta . dL/dtheta
 };
@@ -1596,8 +1596,10 @@ void orc_render_grad(void* s, const float* cam, uint32_t width, uint32_t height,
     {
         std::vector<double> local(n, 0.0);
         GradPath G;
-        G.n = n;
-        G.beta_d.assign(3 * n, 0.0);
+        // the throughput depends on the material parameters only (texels enter
+        // through emitted radiance, added directly in add_term)
+        G.n = sc->materials.size() * 6;
+        G.beta_d.assign(3 * G.n, 0.0);
         G.grad = &local;
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 4)

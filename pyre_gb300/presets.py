@@ -445,3 +445,26 @@ def adjoint_check_scene():
     px[2, 5] = [20.0, 18.0, 14.0]  # a bright texel
     sc.env = HdriEnvironmentLight(16, 8, px, 1.0)
     return sc, studio_ref_camera(48, 48)
+
+
+def fd_check_scene():
+    """A scene for finite-difference gradient checks: a Lambertian ground quad, a Disney sphere with metallic
+    0.4 (between dielectric and conductor) and roughness 0.35, a dielectric Disney sphere with roughness 0.6,
+    a 16x8 HDRI with one bright (sun) texel and dim sky texels, and a quad light above; 64x64 pinhole camera.
+    Returns (scene, camera)."""
+    sc = Scene()
+    sc.materials.append(Lambertian([0.6, 0.58, 0.55]))
+    s = 20.0
+    sc.primitives.append(Primitive(MeshInstance.build(
+        quad_mesh([(-s, 0, -s), (s, 0, -s), (s, 0, s), (-s, 0, s)], (0, 1, 0))), 0))
+    sc.materials.append(DisneyBsdf([0.75, 0.45, 0.25], 0.4, 0.35, 0.5))
+    sc.primitives.append(Primitive(MeshInstance.build(make_uv_sphere((-0.35, 0.35, 0.0), 0.35, 32, 16)), 1))
+    sc.materials.append(DisneyBsdf([0.2, 0.5, 0.75], 0.0, 0.6, 0.5))
+    sc.primitives.append(Primitive(MeshInstance.build(make_uv_sphere((0.4, 0.3, -0.1), 0.3, 32, 16)), 2))
+    rng = np.random.default_rng(5)
+    px = (0.2 + 0.3 * rng.random((8, 16, 3))).astype(F32)
+    px[2, 5] = [30.0, 27.0, 21.0]  # the sun texel
+    sc.env = HdriEnvironmentLight(16, 8, px, 1.0)
+    sc.lights.append(DiffuseAreaQuadLight((-0.5, 2.0, -0.5), (1.0, 0, 0), (0, 0, 1.0), (4.0, 4.0, 4.0)))
+    cam = PinholeCamera.look_at((0, 0.9, 2.2), (0, 0.3, 0), (0, 1, 0), 40.0, 1.0)
+    return sc, cam

@@ -403,13 +403,18 @@ class CudaIntegrator:
 
     def render_batch(self, dscene: DeviceScene, jobs: list, wave_paths: int = 0, use_graph: int = 0,
                      block_size: int = 0, sort_by_material: int = 0, refill_lanes: int = 0,
-                     bvh_width: int = 0) -> list:
-        """jobs: dicts with part, camera, width, height, spp, spp_begin (0), integrator -> list of Films."""
-        films, cjobs = [], []
-        for jb in jobs:
+                     bvh_width: int = 0, films: list | None = None) -> list:
+        """jobs: dicts with part, camera, width, height, spp, spp_begin (0), integrator -> list of Films.
+        `films` (one Film per job, of its size) are filled in place instead of new ones."""
+        cjobs = []
+        if films is None:
+            films = [Film(jb["width"], jb["height"]) for jb in jobs]
+        if len(films) != len(jobs):
+            raise ValueError("one film per job")
+        for jb, film in zip(jobs, films):
             w, h = jb["width"], jb["height"]
-            film = Film(w, h)
-            films.append(film)
+            if film.radiance.shape != (h, w, 3):
+                raise ValueError("film size differs from the job's image size")
             it = jb.get("integrator", PathIntegrator())
             b = N.BatchJob()
             b.part = jb["part"]

@@ -13,28 +13,35 @@ pytestmark = pytest.mark.gpu
 
 
 def test_injected_allocation_failures(gpu_ctx):
-    sc, it = P.cornell_ref(), PathIntegrator(8, 3)
-    ds = gpu_ctx.upload(sc)
-    small = gpu_ctx.render(ds, P.cornell_ref_camera(32, 24), it, 32, 24, 2)
-    # a larger render needs a larger workspace: its allocation fails
-    gpu_ctx.lib.pyre_inject_alloc_failure(gpu_ctx.handle, 0)
-    with pytest.raises(PyreError) as e:
-        gpu_ctx.render(ds, P.cornell_ref_camera(640, 480), it, 640, 480, 4)
-    assert e.value.code == PYRE_ERR_OOM
-    again = gpu_ctx.render(ds, P.cornell_ref_camera(32, 24), it, 32, 24, 2)
-    np.testing.assert_array_equal(again.radiance, small.radiance)
-    # a scene upload that fails part-way frees what it had allocated
-    for after in (0, 2, 5):
-        gpu_ctx.lib.pyre_inject_alloc_failure(gpu_ctx.handle, after)
+    # a context of its own: how large the shared context's workspace has grown depends on the tests before
+    from pyre_gb300.scene import CudaIntegrator
+    ctx = CudaIntegrator(0)
+    try:
+        sc, it = P.cornell_ref(), PathIntegrator(8, 3)
+        ds = ctx.upload(sc)
+        small = ctx.render(ds, P.cornell_ref_camera(32, 24), it, 32, 24, 2)
+        # a larger render needs a larger workspace: its allocation fails
+        ctx.lib.pyre_inject_alloc_failure(ctx.handle, 0)
         with pytest.raises(PyreError) as e:
-            gpu_ctx.upload(sc)
+            ctx.render(ds, P.cornell_ref_camera(640, 480), it, 640, 480, 4)
         assert e.value.code == PYRE_ERR_OOM
-    gpu_ctx.lib.pyre_inject_alloc_failure(gpu_ctx.handle, -1)
-    ds2 = gpu_ctx.upload(sc)
-    np.testing.assert_array_equal(gpu_ctx.render(ds2, P.cornell_ref_camera(32, 24), it, 32, 24, 2).radiance,
-                                  small.radiance)
-    ds.close()
-    ds2.close()
+        again = ctx.render(ds, P.cornell_ref_camera(32, 24), it, 32, 24, 2)
+        np.testing.assert_array_equal(again.radiance, small.radiance)
+        # a scene upload that fails part-way frees what it had allocated
+        for after in (0, 2, 5):
+            ctx.lib.pyre_inject_alloc_failure(ctx.handle, after)
+            with pytest.raises(PyreError) as e:
+                ctx.upload(sc)
+            assert e.value.code == PYRE_ERR_OOM
+        ctx.lib.pyre_inject_alloc_failure(ctx.handle, -1)
+        ds2 = ctx.upload(sc)
+        np.testing.assert_array_equal(ctx.render(ds2, P.cornell_ref_camera(32, 24), it, 32, 24, 2).radiance,
+                                      small.radiance)
+        ds.close()
+        ds2.close()
+    finally:
+        ctx.lib.pyre_inject_alloc_failure(ctx.handle, -1)
+        ctx.close()
 
 
 def _deep_bvh(levels: int):
