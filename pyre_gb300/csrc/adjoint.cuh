@@ -74,6 +74,99 @@ struct D6x3 {
     D6 x, y, z;
 };
 
+#ifndef PYRE_JAC_CLOSED_FORM
+#define PYRE_JAC_CLOSED_FORM 1
+#endif
+
+#if PYRE_JAC_CLOSED_FORM
+// Parameter Jacobian of f(wo, wi) for one material, J[c][k] = d f_c / d param_k,
+// in closed form over the formulas of bsdf_eval (material.rs:52-58, 125-155,
+// helpers 232-281). With kd = (1-m)/pi fd_v fd_l, fd = 1 + (fd90-1) p5(cos),
+// fd90 = 0.5 + 2 r cos_d^2, DG = D G / (4 cos_o cos_i), F_c = f0_c (1-p5) + p5
+// and f0_c = 0.08 s (1-m) + base_c m:
+//   d/d base_c   = kd + m (1-p5) DG                      (diagonal in c)
+//   d/d m        = -base_c fd_v fd_l / pi + (base_c - 0.08 s)(1-p5) DG
+//   d/d r        = base_c (1-m)/pi 2 cos_d^2 (p5_o fd_l + fd_v p5_i)
+//                  + F_c / (4 cos_o cos_i) (dD/da2 G + D dG/da2) da2/dr
+//   d/d s        = 0.08 (1-m)(1-p5) DG
+// with a2 = alpha^2, alpha = max(r^2, 1e-3), dD/da2 = (den - 2 a2 hz^2) / (pi den^3)
+// for den = (a2-1) hz^2 + 1, dG/da2 = -G^2 (dL_o + dL_i) and
+// dL/da2 = tan2 / (4 sqrt(1 + a2 tan2)). About a sixth of the arithmetic of
+// carrying six dual-number tangents through the same formulas.
+// Not inlined: it is called from several sites of a large kernel, and one
+// out-of-line copy keeps the instruction footprint small.
+static __device__ __noinline__ void bsdf_eval_jac(const Bsdf& b, f3 wo, f3 wi, float J[3][PYRE_NPARAM]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int k = 0; k < PYRE_NPARAM; ++k) J[c][k] = 0.0f;
+    if (wo.z <= 0.0f || wi.z <= 0.0f) return;
+    if (b.kind == PYRE_MAT_LAMBERTIAN) {  // f = albedo / pi
+        J[0][0] = J[1][1] = J[2][2] = 1.0f / PYRE_PI;
+        return;
+    }
+    const f3 h = normalize_or_zero3(wo + wi);
+    if (len2(h) < 1e-10f) return;
+    const float base[3] = {b.base.x, b.base.y, b.base.z};
+    const float m = b.metallic, r = b.roughness, sp = b.specular;
+    if (!(m >= 1.0f)) {  // diffuse (material.rs:125-138)
+        const float cos_d = clampf_(dot3(wi, h), 0.0f, 1.0f);
+        const float c2 = cos_d * cos_d;
+        const float fd90 = 0.5f + r * (2.0f * c2);
+        const float pv = powi5(fmaxf(1.0f - wo.z, 0.0f)), pl = powi5(fmaxf(1.0f - wi.z, 0.0f));
+        const float fd_v = 1.0f + (fd90 - 1.0f) * pv, fd_l = 1.0f + (fd90 - 1.0f) * pl;
+        const float vl = fd_v * fd_l * (1.0f / PYRE_PI);
+        const float kd = (1.0f - m) * vl;
+        const float kr = (1.0f - m) * (1.0f / PYRE_PI) * (2.0f * c2) * (pv * fd_l + fd_v * pl);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            J[c][c] = kd;
+            J[c][3] = -base[c] * vl;
+            J[c][4] = base[c] * kr;
+        }
+    }
+    if (h.z <= 0.0f) return;
+    // specular (material.rs:142-155)
+    const float r2 = r * r;
+    const bool clamped = !(r2 >= 1e-3f);
+    const float alpha = clamped ? 1e-3f : r2;
+    const float a2 = alpha * alpha;
+    const float da2_dr = clamped ? 0.0f : 2.0f * alpha * (2.0f * r);
+    const float hz2 = h.z * h.z;
+    const float den = (a2 - 1.0f) * hz2 + 1.0f;
+    const float d = a2 / ((den * den) * PYRE_PI);
+    const float dd = (den - 2.0f * a2 * hz2) / (PYRE_PI * den * den * den);
+    float lam_sum = 0.0f, dlam_sum = 0.0f;
+    const f3 v2[2] = {wo, wi};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const float cos2 = v2[q].z * v2[q].z;
+        if (cos2 >= 1.0f) continue;
+        const float tan2 = (1.0f - cos2) / fmaxf(cos2, 1e-8f);
+        const float root = sqrtf(1.0f + a2 * tan2);
+        lam_sum += 0.5f * (root - 1.0f);
+        dlam_sum += root > 0.0f ? 0.25f * tan2 / root : 0.0f;
+    }
+    const float g = 1.0f / (1.0f + lam_sum);
+    const float dg = -g * g * dlam_sum;
+    const float cd = clampf_(fmaxf(dot3(wi, h), 0.0f), 0.0f, 1.0f);
+    const float p5 = powi5(1.0f - cd);
+    const float inv = 1.0f / (4.0f * wo.z * wi.z);
+    const float dgi = d * g * inv;                          // D G / (4 cos_o cos_i)
+    const float dr_s = (dd * g + d * dg) * inv * da2_dr;    // d(D G / (4 cos cos)) / d r
+    const float diel = 0.08f * sp;
+    const float q5 = 1.0f - p5;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float f0 = diel * (1.0f - m) + base[c] * m;
+        const float F = f0 + (1.0f - f0) * p5;
+        J[c][c] += m * q5 * dgi;
+        J[c][3] += (base[c] - diel) * q5 * dgi;
+        J[c][4] += F * dr_s;
+        J[c][5] = 0.08f * (1.0f - m) * q5 * dgi;
+    }
+}
+#else
 // Value and parameter Jacobian of f(wo, wi) for one material:
 // J[c][k] = d f_c / d param_k.
 // Not inlined: it is called from several sites of a large kernel, and one
@@ -137,6 +230,7 @@ static __device__ __noinline__ void bsdf_eval_jac(const Bsdf& b, f3 wo, f3 wi, f
 #pragma unroll
     for (int k = 0; k < PYRE_NPARAM; ++k) { J[0][k] = f.x.d[k]; J[1][k] = f.y.d[k]; J[2][k] = f.z.d[k]; }
 }
+#endif
 
 // The four texels and weights of env_texture's bilinear lookup (light.rs:290-314).
 __device__ __forceinline__ void env_texel_weights(const DevEnv& E, f2 uv, uint32_t idx[4], float wt[4]) {

@@ -468,6 +468,7 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
         }
     }
     const int32_t node_off = (int32_t)blas.n_nodes;  // top-level nodes follow the device-built ones
+    const int32_t tlas_first = node_off + (int32_t)nodes.size();  // every part's top level, contiguous
 
     // ---- instances and one top-level BVH per part over their swept bounds
     std::vector<DevInstance> inst;
@@ -602,6 +603,9 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     D.inst = d_inst;
     D.n_inst = (uint32_t)inst.size();
     D.tlas_root = tlas_root;
+    D.tlas_first = tlas_first;
+    D.tlas_count = (uint32_t)(node_off + (int32_t)nodes.size() - tlas_first);
+    D.tlas_smem = D.tlas_count <= PYRE_TLAS_SMEM_NODES ? D.tlas_count : 0u;
     uint32_t* d_index = nullptr;
     if ((rc = upload(ctx, sc, index, &d_index)) != PYRE_OK) return fail(rc);
     D.index = d_index;

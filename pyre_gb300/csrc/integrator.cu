@@ -972,8 +972,11 @@ struct Launch {
 // block_size (0 = defaults: 256 for raygen and accumulate, 224 for the
 // forward shade, 128 for the traces) sets them all, capped at 224 for the
 // forward shade and 128 for the traces.
+// Dynamic shared memory of the traversal kernels: the staged top-level nodes.
+inline size_t trace_smem(const DevScene& S) { return (size_t)S.tlas_smem * 4 * sizeof(float4); }
+
 template <bool BATCH>
-Launch make_launch(pyre_ctx* ctx, uint32_t block_size, int width) {
+Launch make_launch(pyre_ctx* ctx, uint32_t block_size, int width, size_t tsmem) {
     Launch L;
     if (block_size) {
         const int b = (int)std::max(32u, std::min(256u, block_size / 32 * 32));
@@ -983,12 +986,12 @@ Launch make_launch(pyre_ctx* ctx, uint32_t block_size, int width) {
     }
     L.grid_raygen = grid_for(ctx, k_raygen<BATCH>, L.block_stage);
     L.grid_shade = grid_for(ctx, k_shade<BATCH>, L.block_shade);
-    L.grid_extend = width == 8 ? grid_for(ctx, k_extend<BATCH, 8>, L.block_trace)
-                    : width == 4 ? grid_for(ctx, k_extend<BATCH, 4>, L.block_trace)
-                                 : grid_for(ctx, k_extend<BATCH, 2>, L.block_trace);
-    L.grid_shadow = width == 8 ? grid_for(ctx, k_shadow<BATCH, 8>, L.block_trace)
-                    : width == 4 ? grid_for(ctx, k_shadow<BATCH, 4>, L.block_trace)
-                                 : grid_for(ctx, k_shadow<BATCH, 2>, L.block_trace);
+    L.grid_extend = width == 8 ? grid_for(ctx, k_extend<BATCH, 8>, L.block_trace, tsmem)
+                    : width == 4 ? grid_for(ctx, k_extend<BATCH, 4>, L.block_trace, tsmem)
+                                 : grid_for(ctx, k_extend<BATCH, 2>, L.block_trace, tsmem);
+    L.grid_shadow = width == 8 ? grid_for(ctx, k_shadow<BATCH, 8>, L.block_trace, tsmem)
+                    : width == 4 ? grid_for(ctx, k_shadow<BATCH, 4>, L.block_trace, tsmem)
+                                 : grid_for(ctx, k_shadow<BATCH, 2>, L.block_trace, tsmem);
     L.grid_acc = BATCH ? grid_for(ctx, k_accumulate_batch, L.block_stage) : grid_for(ctx, k_accumulate, L.block_stage);
     L.grid_sort = grid_for(ctx, k_sort_scatter, 256);
     return L;
@@ -1014,16 +1017,18 @@ enum { STAGE_EXTEND = 0, STAGE_SHADE = 1, STAGE_SHADOW = 2, STAGE_OTHER = 3, STA
 template <bool BATCH>
 void launch_extend(cudaStream_t st, const Launch& Lc, const DevScene& S, const PathSoA& P, const WaveParams& W,
                    uint32_t d) {
-    if (W.bvh_width == 8) k_extend<BATCH, 8><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
-    else if (W.bvh_width == 4) k_extend<BATCH, 4><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
-    else k_extend<BATCH, 2><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
+    const size_t sm = trace_smem(S);
+    if (W.bvh_width == 8) k_extend<BATCH, 8><<<Lc.grid_extend, Lc.block_trace, sm, st>>>(S, P, W, d);
+    else if (W.bvh_width == 4) k_extend<BATCH, 4><<<Lc.grid_extend, Lc.block_trace, sm, st>>>(S, P, W, d);
+    else k_extend<BATCH, 2><<<Lc.grid_extend, Lc.block_trace, sm, st>>>(S, P, W, d);
 }
 template <bool BATCH>
 void launch_shadow(cudaStream_t st, const Launch& Lc, const DevScene& S, const PathSoA& P, const WaveParams& W,
                    uint32_t d) {
-    if (W.bvh_width == 8) k_shadow<BATCH, 8><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
-    else if (W.bvh_width == 4) k_shadow<BATCH, 4><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
-    else k_shadow<BATCH, 2><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
+    const size_t sm = trace_smem(S);
+    if (W.bvh_width == 8) k_shadow<BATCH, 8><<<Lc.grid_shadow, Lc.block_trace, sm, st>>>(S, P, W, d);
+    else if (W.bvh_width == 4) k_shadow<BATCH, 4><<<Lc.grid_shadow, Lc.block_trace, sm, st>>>(S, P, W, d);
+    else k_shadow<BATCH, 2><<<Lc.grid_shadow, Lc.block_trace, sm, st>>>(S, P, W, d);
 }
 
 // Orders the live paths of depth d by shade_key into P.qsort.
@@ -1204,7 +1209,7 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     S.keep_L = keep;
     if (film->mem == PYRE_MEM_HOST && (rc = ensure_workspace(ctx, ctx->io_ws, film_bytes))) return rc;
 
-    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
+    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width, trace_smem(D));
 
     cudaStream_t st = ctx->stream;
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_r, 0, (size_t)W.npix * sizeof(float4), st));
@@ -1400,7 +1405,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_n, 0, total_pix * sizeof(float4), st));
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
 
-    const Launch Lc = make_launch<true>(ctx, params ? params->block_size : 0u, W.bvh_width);
+    const Launch Lc = make_launch<true>(ctx, params ? params->block_size : 0u, W.bvh_width, trace_smem(D));
 
     PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
     ctx->stage_used = 0;
@@ -1554,7 +1559,7 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     PathSoA S;
     carve_paths((char*)scratch, (size_t)W.npix * K, ns, W.npix, &S);
 
-    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
+    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width, trace_smem(D));
 
     cudaStream_t st = ctx->stream;
     // The array keeps the previous call's contents: clear the sums and counters.
@@ -1591,12 +1596,16 @@ template <bool ANY>
 static void launch_intersect(pyre_ctx* ctx, const DevScene& D, const QueryRays& q, uint32_t n, int width) {
     cudaStream_t st = ctx->stream;
     const int refill = ANY ? PYRE_DEFAULT_REFILL_ANY : PYRE_DEFAULT_REFILL;
+    const size_t sm = trace_smem(D);
     if (width == 8) {
-        k_intersect<ANY, 8><<<grid_for(ctx, k_intersect<ANY, 8>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter, refill);
+        k_intersect<ANY, 8><<<grid_for(ctx, k_intersect<ANY, 8>, 128, sm), 128, sm, st>>>(D, q, n, ctx->d_counter,
+                                                                                          refill);
     } else if (width == 4) {
-        k_intersect<ANY, 4><<<grid_for(ctx, k_intersect<ANY, 4>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter, refill);
+        k_intersect<ANY, 4><<<grid_for(ctx, k_intersect<ANY, 4>, 128, sm), 128, sm, st>>>(D, q, n, ctx->d_counter,
+                                                                                          refill);
     } else {
-        k_intersect<ANY, 2><<<grid_for(ctx, k_intersect<ANY, 2>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter, refill);
+        k_intersect<ANY, 2><<<grid_for(ctx, k_intersect<ANY, 2>, 128, sm), 128, sm, st>>>(D, q, n, ctx->d_counter,
+                                                                                          refill);
     }
 }
 
@@ -1821,7 +1830,7 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     const size_t smem = mat_bytes <= 48 * 1024 ? mat_bytes : 0;
     W.smem_grad = smem ? 1 : 0;
 
-    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
+    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width, trace_smem(D));
     const int grid_adj = grid_for(ctx, k_shade<false, true>, Lc.block_stage, smem);
     const int grid_acc = grid_for(ctx, k_accumulate_adjoint, Lc.block_stage, smem);
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));

@@ -7,7 +7,7 @@ import pytest
 from pyre_gb300 import presets as P
 from pyre_gb300.native import PYRE_ENV_CDF
 from pyre_gb300.scene import (DisneyBsdf, HdriEnvironmentLight, Lambertian, MeshInstance, PathIntegrator, Primitive,
-                              Scene)
+                              Scene)  # noqa: F401
 
 pytestmark = pytest.mark.gpu
 
@@ -133,6 +133,8 @@ def test_adjoint_matches_finite_differences_disney_and_env(gpu_ctx, rr):
     within 3 % of the finite difference."""
     from pyre_gb300.native import PYRE_ENV_CDF
     sc, cam = P.fd_check_scene()
+    # the device scene keeps `sc` and set_materials / set_env replace its fields: perturb copies of the base
+    base = Scene(list(sc.primitives), list(sc.materials), list(sc.lights), sc.env)
     w = h = 64
     it = PathIntegrator(5, 2 if rr else 99)
     spp, blocks, eps = 16384, 16, 1e-3
@@ -143,7 +145,7 @@ def test_adjoint_matches_finite_differences_disney_and_env(gpu_ctx, rr):
              for m in sc.materials]
     gpu_ctx.set_materials(ds, tmats)
     tgt = gpu_ctx.render(ds, cam, it, w, h, 1024, spp_begin=1 << 29, env_sampling=PYRE_ENV_CDF).radiance
-    gpu_ctx.set_materials(ds, sc.materials)
+    gpu_ctx.set_materials(ds, base.materials)
     dl = (2.0 * (ref.astype(np.float64) - tgt) / ref.size).astype(np.float32)
     params = [("mat", m, k) for m in (1, 2) for k in range(6)] + [("env", 2, 5, 0), ("env", 6, 3, 1)]
     if rr:  # the half-metallic sphere and the sun texel
@@ -158,15 +160,15 @@ def test_adjoint_matches_finite_differences_disney_and_env(gpu_ctx, rr):
     for j, p in enumerate(params):
         imgs = {}
         for sign in (1, -1):
-            s2 = _with_param(sc, p, sign * eps)
+            s2 = _with_param(base, p, sign * eps)
             if p[0] == "mat":
                 gpu_ctx.set_materials(ds, s2.materials)
             else:
                 gpu_ctx.set_env(ds, s2.env.pixels, s2.env.intensity)
             imgs[sign] = [gpu_ctx.render(ds, cam, it, w, h, spp, spp_begin=b * spp, env_sampling=PYRE_ENV_CDF)
                           .radiance.astype(np.float64) for b in range(blocks)]
-        gpu_ctx.set_materials(ds, sc.materials)
-        gpu_ctx.set_env(ds, sc.env.pixels, sc.env.intensity)
+        gpu_ctx.set_materials(ds, base.materials)
+        gpu_ctx.set_env(ds, base.env.pixels, base.env.intensity)
         for b in range(blocks):
             FD[b, j] = float(np.sum(d64 * (imgs[1][b] - imgs[-1][b]))) / (2 * eps)
     D = AD - FD
