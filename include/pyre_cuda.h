@@ -382,9 +382,13 @@ typedef struct pyre_batch_job {
  * jobs share the stage kernels and queues, in waves planned on the host
  * (jobs packed in order, each job's samples in sample order, so every film is
  * bit-identical to pyre_render of that job alone). With params->use_graph
- * the whole batch is captured once as one CUDA graph and replayed with a
- * single launch. Uses params->wave_paths (0 = automatic) and use_graph;
- * the per-job fields of params are ignored. */
+ * one wave's bounce loop is captured once as a CUDA graph and replayed for
+ * every wave (the kernels read the wave's segments from device tables).
+ * A job's film is finalized right after the wave that completes it and
+ * copied to the caller's film on a second stream while the later waves
+ * render. Uses params->wave_paths (0 = automatic), use_graph, block_size,
+ * sort_by_material, refill_lanes and bvh_width; the per-view fields of
+ * params are ignored. */
 int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const pyre_batch_job* jobs, uint32_t n_jobs,
                       const pyre_render_params* params);
 

@@ -1,7 +1,8 @@
 // adjoint.cuh — derivatives of the BSDF value with respect to the material
-// parameters (base color r,g,b, metallic, roughness, specular), by forward-mode
-// dual numbers over the same formulas as bsdf_eval (material.rs:52-58,
-// 125-155, helpers 232-281). Directions are not differentiated.
+// parameters (base color r,g,b, metallic, roughness, specular), in closed form
+// over the same formulas as bsdf_eval (material.rs:52-58, 125-155, helpers
+// 232-281), and the gradient reductions of the adjoint replay. Directions are
+// not differentiated.
 #pragma once
 #include "shading.cuh"
 
@@ -9,76 +10,6 @@ namespace pyre {
 
 #define PYRE_NPARAM 6  // base r, g, b, metallic, roughness, specular
 
-struct D6 {
-    float v;
-    float d[PYRE_NPARAM];
-};
-__device__ __forceinline__ D6 dc(float v) {
-    D6 r; r.v = v;
-#pragma unroll
-    for (int k = 0; k < PYRE_NPARAM; ++k) r.d[k] = 0.0f;
-    return r;
-}
-__device__ __forceinline__ D6 dvar(float v, int k) { D6 r = dc(v); r.d[k] = 1.0f; return r; }
-__device__ __forceinline__ D6 operator+(const D6& a, const D6& b) {
-    D6 r; r.v = a.v + b.v;
-#pragma unroll
-    for (int k = 0; k < PYRE_NPARAM; ++k) r.d[k] = a.d[k] + b.d[k];
-    return r;
-}
-__device__ __forceinline__ D6 operator-(const D6& a, const D6& b) {
-    D6 r; r.v = a.v - b.v;
-#pragma unroll
-    for (int k = 0; k < PYRE_NPARAM; ++k) r.d[k] = a.d[k] - b.d[k];
-    return r;
-}
-__device__ __forceinline__ D6 operator*(const D6& a, const D6& b) {
-    D6 r; r.v = a.v * b.v;
-#pragma unroll
-    for (int k = 0; k < PYRE_NPARAM; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
-    return r;
-}
-__device__ __forceinline__ D6 operator/(const D6& a, const D6& b) {
-    D6 r; r.v = a.v / b.v;
-    const float inv2 = 1.0f / (b.v * b.v);
-#pragma unroll
-    for (int k = 0; k < PYRE_NPARAM; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) * inv2;
-    return r;
-}
-__device__ __forceinline__ D6 operator*(const D6& a, float s) {
-    D6 r; r.v = a.v * s;
-#pragma unroll
-    for (int k = 0; k < PYRE_NPARAM; ++k) r.d[k] = a.d[k] * s;
-    return r;
-}
-__device__ __forceinline__ D6 operator*(float s, const D6& a) { return a * s; }
-__device__ __forceinline__ D6 operator+(const D6& a, float s) { D6 r = a; r.v = a.v + s; return r; }
-__device__ __forceinline__ D6 operator+(float s, const D6& a) { return a + s; }
-__device__ __forceinline__ D6 operator-(const D6& a, float s) { D6 r = a; r.v = a.v - s; return r; }
-__device__ __forceinline__ D6 operator-(float s, const D6& a) {
-    D6 r; r.v = s - a.v;
-#pragma unroll
-    for (int k = 0; k < PYRE_NPARAM; ++k) r.d[k] = -a.d[k];
-    return r;
-}
-__device__ __forceinline__ D6 dsqrt(const D6& a) {
-    D6 r; r.v = sqrtf(a.v);
-    const float g = r.v > 0.0f ? 0.5f / r.v : 0.0f;
-#pragma unroll
-    for (int k = 0; k < PYRE_NPARAM; ++k) r.d[k] = a.d[k] * g;
-    return r;
-}
-__device__ __forceinline__ D6 dmax(const D6& a, float b) { return a.v >= b ? a : dc(b); }
-
-struct D6x3 {
-    D6 x, y, z;
-};
-
-#ifndef PYRE_JAC_CLOSED_FORM
-#define PYRE_JAC_CLOSED_FORM 1
-#endif
-
-#if PYRE_JAC_CLOSED_FORM
 // Parameter Jacobian of f(wo, wi) for one material, J[c][k] = d f_c / d param_k,
 // in closed form over the formulas of bsdf_eval (material.rs:52-58, 125-155,
 // helpers 232-281). With kd = (1-m)/pi fd_v fd_l, fd = 1 + (fd90-1) p5(cos),
@@ -92,7 +23,8 @@ struct D6x3 {
 // with a2 = alpha^2, alpha = max(r^2, 1e-3), dD/da2 = (den - 2 a2 hz^2) / (pi den^3)
 // for den = (a2-1) hz^2 + 1, dG/da2 = -G^2 (dL_o + dL_i) and
 // dL/da2 = tan2 / (4 sqrt(1 + a2 tan2)). About a sixth of the arithmetic of
-// carrying six dual-number tangents through the same formulas.
+// carrying six dual-number tangents through the same formulas, and the
+// same speed on the adjoint replay (measured), with a smaller code footprint.
 // Not inlined: it is called from several sites of a large kernel, and one
 // out-of-line copy keeps the instruction footprint small.
 static __device__ __noinline__ void bsdf_eval_jac(const Bsdf& b, f3 wo, f3 wi, float J[3][PYRE_NPARAM]) {
@@ -166,71 +98,6 @@ static __device__ __noinline__ void bsdf_eval_jac(const Bsdf& b, f3 wo, f3 wi, f
         J[c][5] = 0.08f * (1.0f - m) * q5 * dgi;
     }
 }
-#else
-// Value and parameter Jacobian of f(wo, wi) for one material:
-// J[c][k] = d f_c / d param_k.
-// Not inlined: it is called from several sites of a large kernel, and one
-// out-of-line copy keeps the instruction footprint small.
-static __device__ __noinline__ void bsdf_eval_jac(const Bsdf& b, f3 wo, f3 wi, float J[3][PYRE_NPARAM]) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int k = 0; k < PYRE_NPARAM; ++k) J[c][k] = 0.0f;
-    if (b.kind == PYRE_MAT_LAMBERTIAN) {  // f = albedo / pi
-        if (wo.z <= 0.0f || wi.z <= 0.0f) return;
-        J[0][0] = J[1][1] = J[2][2] = 1.0f / PYRE_PI;
-        return;
-    }
-    const D6 br = dvar(b.base.x, 0), bg = dvar(b.base.y, 1), bb = dvar(b.base.z, 2);
-    const D6 metal = dvar(b.metallic, 3), rough = dvar(b.roughness, 4), spec = dvar(b.specular, 5);
-    D6x3 f;
-    f.x = dc(0.0f); f.y = dc(0.0f); f.z = dc(0.0f);
-    // diffuse (material.rs:125-138)
-    if (!(wo.z <= 0.0f || wi.z <= 0.0f || b.metallic >= 1.0f)) {
-        f3 h = normalize_or_zero3(wo + wi);
-        if (!(len2(h) < 1e-10f)) {
-            const float cos_d = clampf_(dot3(wi, h), 0.0f, 1.0f);
-            const D6 fd90 = 0.5f + rough * (2.0f * cos_d * cos_d);
-            const float pv = powi5(fmaxf(1.0f - wo.z, 0.0f)), pl = powi5(fmaxf(1.0f - wi.z, 0.0f));
-            const D6 fd_v = 1.0f + (fd90 - 1.0f) * pv;
-            const D6 fd_l = 1.0f + (fd90 - 1.0f) * pl;
-            const D6 k = (1.0f - metal) * (1.0f / PYRE_PI) * fd_v * fd_l;
-            f.x = br * k; f.y = bg * k; f.z = bb * k;
-        }
-    }
-    // specular (material.rs:142-155)
-    if (!(wo.z <= 0.0f || wi.z <= 0.0f)) {
-        f3 h = normalize_or_zero3(wo + wi);
-        if (!(len2(h) < 1e-10f || h.z <= 0.0f)) {
-            const D6 alpha = dmax(rough * rough, 1e-3f);
-            const D6 a2 = alpha * alpha;
-            const D6 denom = (a2 - 1.0f) * (h.z * h.z) + 1.0f;
-            const D6 d = a2 / ((denom * denom) * PYRE_PI);
-            // lambda(v) = 0.5 * (-1 + sqrt(1 + a2 * tan2))
-            auto lam = [&](f3 v) {
-                const float cos2 = v.z * v.z;
-                if (cos2 >= 1.0f) return dc(0.0f);
-                const float tan2 = (1.0f - cos2) / fmaxf(cos2, 1e-8f);
-                return 0.5f * (dsqrt(1.0f + a2 * tan2) - 1.0f);
-            };
-            const D6 g = dc(1.0f) / (1.0f + lam(wo) + lam(wi));
-            const float c = clampf_(fmaxf(dot3(wi, h), 0.0f), 0.0f, 1.0f);
-            const float p5 = powi5(1.0f - c);
-            const D6 diel = spec * 0.08f;
-            // f0 = lerp(diel, base, metallic) = diel*(1-m) + base*m; F = f0 + (1-f0)*p5
-            const D6 one_m = 1.0f - metal;
-            const float inv = 1.0f / (4.0f * wo.z * wi.z);
-            const D6 f0r = diel * one_m + br * metal, f0g = diel * one_m + bg * metal, f0b = diel * one_m + bb * metal;
-            const D6 dg = d * g * inv;
-            f.x = f.x + (f0r + (1.0f - f0r) * p5) * dg;
-            f.y = f.y + (f0g + (1.0f - f0g) * p5) * dg;
-            f.z = f.z + (f0b + (1.0f - f0b) * p5) * dg;
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < PYRE_NPARAM; ++k) { J[0][k] = f.x.d[k]; J[1][k] = f.y.d[k]; J[2][k] = f.z.d[k]; }
-}
-#endif
 
 // The four texels and weights of env_texture's bilinear lookup (light.rs:290-314).
 __device__ __forceinline__ void env_texel_weights(const DevEnv& E, f2 uv, uint32_t idx[4], float wt[4]) {

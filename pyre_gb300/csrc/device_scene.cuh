@@ -84,17 +84,11 @@ struct DevScene {
     // root of each instance slot
     const float4* wnodes;
     const int32_t* wroot;
-    // the top-level nodes (every part's) are nodes [tlas_first, tlas_first + tlas_count); when there are at
-    // most PYRE_TLAS_SMEM_NODES of them the traversal kernels stage them in shared memory (tlas_smem =
-    // tlas_count, else 0) and launch with tlas_smem * 64 bytes of dynamic shared memory
-    int32_t tlas_first;
-    uint32_t tlas_count;
-    uint32_t tlas_smem;
+    // the instances' (swept) world bounds, for the coarse spatial key of the ray reordering:
+    // cell = (o - cell_lo) * cell_scale, 8 x 4 x 4 cells
+    float cell_lo[3], cell_scale[3];
 };
 
-#ifndef PYRE_TLAS_SMEM_NODES
-#define PYRE_TLAS_SMEM_NODES 128  // 8 KB per block
-#endif
 
 struct TraceRay {
     f3 o, d;
@@ -262,13 +256,6 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
         --sp;
         return (SK > 0 && sp < SK) ? sstack[sp][threadIdx.x] : stack[sp - SK];
     };
-    // The top-level BVH in shared memory: every block loads it once (the kernels are persistent), and the
-    // top-level steps, 29 % of all node steps on the 1080p studio frame, read it from there.
-    extern __shared__ float4 s_tlas[];
-    const uint32_t n_tlas = S.tlas_smem;
-    for (uint32_t k = threadIdx.x; k < 4 * n_tlas; k += blockDim.x)
-        s_tlas[k] = __ldg(S.nodes + 4 * (size_t)S.tlas_first + k);
-    __syncthreads();
     int node = PYRE_NODE_NONE;
     int inst = -1;
     f3 o = r.o;
@@ -402,19 +389,9 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                 node = ent[0];
                 continue;
             }
-            const int nidx = node & ~PYRE_TAG_TOP;
-            float4 na, nb, nc;
-            int4 nd;
-            if (top && n_tlas) {
-                const float4* N = s_tlas + 4 * (nidx - S.tlas_first);
-                na = N[0]; nb = N[1]; nc = N[2];
-                const float4 q = N[3];
-                nd = make_int4(__float_as_int(q.x), __float_as_int(q.y), __float_as_int(q.z), __float_as_int(q.w));
-            } else {
-                const float4* N = S.nodes + 4 * (size_t)nidx;
-                na = __ldg(N); nb = __ldg(N + 1); nc = __ldg(N + 2);
-                nd = __ldg(reinterpret_cast<const int4*>(N + 3));
-            }
+            const float4* N = S.nodes + 4 * (size_t)(node & ~PYRE_TAG_TOP);
+            const float4 na = __ldg(N), nb = __ldg(N + 1), nc = __ldg(N + 2);
+            const int4 nd = __ldg(reinterpret_cast<const int4*>(N + 3));
             float e0, e1;
             const bool h0 = nd.x >= 0 && slab(na.x, na.y, na.z, na.w, nc.x, nc.y, o, inv, r.tmin, best_t, &e0);
             const bool h1 = nd.y >= 0 && slab(nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, o, inv, r.tmin, best_t, &e1);

@@ -32,6 +32,9 @@ namespace cg = cooperative_groups;
 namespace pyre {
 
 #define PYRE_MAX_DEPTH 64
+#ifndef PYRE_SORT_RAYS
+#define PYRE_SORT_RAYS 0  // extend traces the rays of depth >= 1 grouped by ray_key
+#endif
 #define PYRE_SORT_BINS 1024  // shade-queue sort keys: escaped, light hit, then materials
 
 struct WaveCtl {
@@ -92,6 +95,7 @@ struct WaveParams {
     int refill_any;      // the same for the any-hit (shadow) traversal
     int sort;            // shade reads the live paths sorted by material (P.qsort)
     int bvh_width;       // instance BVH width of the traversal kernels: 2, 4 or 8
+    int sort_rays;       // extend reads the live rays of depth >= 1 grouped by (origin cell, direction octant)
     // progressive accumulation (pyre_render_progressive): crop npix x 3 running
     // mean of the radiance, updated once per sample in sample order
     float* prog_mean;
@@ -300,9 +304,11 @@ struct ExtendRays {
     const WaveParams* W;
     const uint32_t* qin;  // live-path queue; null at depth 0 (every path of the wave)
     uint32_t depth;
-    // ray j of the queue sits at queue position j (depth 0: path tiled_path(j))
+    const uint32_t* order;  // queue positions grouped by ray key (reordered rays), or null
+    // ray j of the queue sits at queue position j (depth 0: path tiled_path(j)); with `order` the j-th ray
+    // traced is the one at queue position order[j], and its hit goes back to that position
     __device__ __forceinline__ uint32_t load(uint32_t j, TraceRay& r, int32_t& root) const {
-        const uint32_t p = qin ? j : (BATCH ? j : tiled_path(*W, j));
+        const uint32_t p = order ? __ldcs(order + j) : qin ? j : (BATCH ? j : tiled_path(*W, j));
         const float4 ro = __ldcs(P->ray_o[depth & 1] + p), rd = __ldcs(P->ray_d[depth & 1] + p);
         r.o = mk3(ro.x, ro.y, ro.z);
         r.d = mk3(rd.x, rd.y, rd.z);
@@ -331,7 +337,8 @@ struct ExtendRays {
 // unconstrained 70-register build by 2 %; 10 blocks (48 registers) lose 2 %.
 template <bool BATCH, int WIDTH>
 __global__ void __launch_bounds__(128, 9) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
-    ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1], depth};
+    ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1], depth,
+                          (W.sort_rays && depth > 0) ? P.qsort : nullptr};
     trace_stream<false, WIDTH>(S, src, P.ctl->count[depth], &P.ctl->fetch[2 * depth], W.refill);
 }
 
@@ -456,6 +463,46 @@ __global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
         if (lane == leader) base = atomicAdd(&P.ctl->sort_off[key], (uint32_t)__popc(peers));
         base = __shfl_sync(peers, base, leader);
         P.qsort[base + __popc(peers & below)] = j;  // the queue position
+    }
+}
+
+// -------------------------------------------------------- ray reordering --
+// Extend at depth >= 1 can trace the live rays grouped by a coarse key: the
+// cell of the origin in an 8 x 4 x 4 grid over the instances' bounds, then
+// the direction's octant (1024 keys). A counting sort gives the order; within
+// a key the rays keep roughly their queue order, which follows the pixels, so
+// a warp gets rays from nearby origins heading the same way. Hits go back to
+// the rays' own queue positions, so shade and the results do not change.
+__device__ __forceinline__ uint32_t ray_key(const DevScene& S, const float4& o, const float4& d) {
+    const int cx = min(max((int)((o.x - S.cell_lo[0]) * S.cell_scale[0]), 0), 7);
+    const int cy = min(max((int)((o.y - S.cell_lo[1]) * S.cell_scale[1]), 0), 3);
+    const int cz = min(max((int)((o.z - S.cell_lo[2]) * S.cell_scale[2]), 0), 3);
+    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    return ((uint32_t)(cx << 4 | cy << 2 | cz) << 3) | oct;
+}
+
+__global__ void k_raysort_count(DevScene S, PathSoA P, uint32_t depth) {
+    const uint32_t n = P.ctl->count[depth];
+    const int lane = threadIdx.x & 31;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t key = ray_key(S, P.ray_o[depth & 1][j], P.ray_d[depth & 1][j]);
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        if (lane == __ffs(peers) - 1) atomicAdd(&P.ctl->sort_hist[key], (uint32_t)__popc(peers));
+    }
+}
+
+__global__ void k_raysort_scatter(DevScene S, PathSoA P, uint32_t depth) {
+    const uint32_t n = P.ctl->count[depth];
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t key = ray_key(S, P.ray_o[depth & 1][j], P.ray_d[depth & 1][j]);
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&P.ctl->sort_off[key], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        P.qsort[base + __popc(peers & below)] = j;
     }
 }
 
@@ -813,8 +860,10 @@ __global__ void k_accumulate_batch(PathSoA P, WaveParams W) {
 }
 
 // Batch: per-job means into a staging film laid out like the accumulators.
-__global__ void k_finalize_batch(PathSoA P, const DevJob* jobs, uint32_t n_jobs, uint32_t total, float* out) {
-    for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < total; a += gridDim.x * blockDim.x) {
+// Means of the batch accumulators [a0, a1) (whole jobs) into the staging film.
+__global__ void k_finalize_batch(PathSoA P, const DevJob* jobs, uint32_t n_jobs, uint32_t total, uint32_t a0,
+                                 uint32_t a1, float* out) {
+    for (uint32_t a = a0 + blockIdx.x * blockDim.x + threadIdx.x; a < a1; a += gridDim.x * blockDim.x) {
         uint32_t lo = 0, hi = n_jobs - 1;
         while (lo < hi) {
             uint32_t mid = (lo + hi + 1) / 2;
@@ -972,11 +1021,8 @@ struct Launch {
 // block_size (0 = defaults: 256 for raygen and accumulate, 224 for the
 // forward shade, 128 for the traces) sets them all, capped at 224 for the
 // forward shade and 128 for the traces.
-// Dynamic shared memory of the traversal kernels: the staged top-level nodes.
-inline size_t trace_smem(const DevScene& S) { return (size_t)S.tlas_smem * 4 * sizeof(float4); }
-
 template <bool BATCH>
-Launch make_launch(pyre_ctx* ctx, uint32_t block_size, int width, size_t tsmem) {
+Launch make_launch(pyre_ctx* ctx, uint32_t block_size, int width) {
     Launch L;
     if (block_size) {
         const int b = (int)std::max(32u, std::min(256u, block_size / 32 * 32));
@@ -986,12 +1032,12 @@ Launch make_launch(pyre_ctx* ctx, uint32_t block_size, int width, size_t tsmem) 
     }
     L.grid_raygen = grid_for(ctx, k_raygen<BATCH>, L.block_stage);
     L.grid_shade = grid_for(ctx, k_shade<BATCH>, L.block_shade);
-    L.grid_extend = width == 8 ? grid_for(ctx, k_extend<BATCH, 8>, L.block_trace, tsmem)
-                    : width == 4 ? grid_for(ctx, k_extend<BATCH, 4>, L.block_trace, tsmem)
-                                 : grid_for(ctx, k_extend<BATCH, 2>, L.block_trace, tsmem);
-    L.grid_shadow = width == 8 ? grid_for(ctx, k_shadow<BATCH, 8>, L.block_trace, tsmem)
-                    : width == 4 ? grid_for(ctx, k_shadow<BATCH, 4>, L.block_trace, tsmem)
-                                 : grid_for(ctx, k_shadow<BATCH, 2>, L.block_trace, tsmem);
+    L.grid_extend = width == 8 ? grid_for(ctx, k_extend<BATCH, 8>, L.block_trace)
+                    : width == 4 ? grid_for(ctx, k_extend<BATCH, 4>, L.block_trace)
+                                 : grid_for(ctx, k_extend<BATCH, 2>, L.block_trace);
+    L.grid_shadow = width == 8 ? grid_for(ctx, k_shadow<BATCH, 8>, L.block_trace)
+                    : width == 4 ? grid_for(ctx, k_shadow<BATCH, 4>, L.block_trace)
+                                 : grid_for(ctx, k_shadow<BATCH, 2>, L.block_trace);
     L.grid_acc = BATCH ? grid_for(ctx, k_accumulate_batch, L.block_stage) : grid_for(ctx, k_accumulate, L.block_stage);
     L.grid_sort = grid_for(ctx, k_sort_scatter, 256);
     return L;
@@ -1017,18 +1063,16 @@ enum { STAGE_EXTEND = 0, STAGE_SHADE = 1, STAGE_SHADOW = 2, STAGE_OTHER = 3, STA
 template <bool BATCH>
 void launch_extend(cudaStream_t st, const Launch& Lc, const DevScene& S, const PathSoA& P, const WaveParams& W,
                    uint32_t d) {
-    const size_t sm = trace_smem(S);
-    if (W.bvh_width == 8) k_extend<BATCH, 8><<<Lc.grid_extend, Lc.block_trace, sm, st>>>(S, P, W, d);
-    else if (W.bvh_width == 4) k_extend<BATCH, 4><<<Lc.grid_extend, Lc.block_trace, sm, st>>>(S, P, W, d);
-    else k_extend<BATCH, 2><<<Lc.grid_extend, Lc.block_trace, sm, st>>>(S, P, W, d);
+    if (W.bvh_width == 8) k_extend<BATCH, 8><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
+    else if (W.bvh_width == 4) k_extend<BATCH, 4><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
+    else k_extend<BATCH, 2><<<Lc.grid_extend, Lc.block_trace, 0, st>>>(S, P, W, d);
 }
 template <bool BATCH>
 void launch_shadow(cudaStream_t st, const Launch& Lc, const DevScene& S, const PathSoA& P, const WaveParams& W,
                    uint32_t d) {
-    const size_t sm = trace_smem(S);
-    if (W.bvh_width == 8) k_shadow<BATCH, 8><<<Lc.grid_shadow, Lc.block_trace, sm, st>>>(S, P, W, d);
-    else if (W.bvh_width == 4) k_shadow<BATCH, 4><<<Lc.grid_shadow, Lc.block_trace, sm, st>>>(S, P, W, d);
-    else k_shadow<BATCH, 2><<<Lc.grid_shadow, Lc.block_trace, sm, st>>>(S, P, W, d);
+    if (W.bvh_width == 8) k_shadow<BATCH, 8><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
+    else if (W.bvh_width == 4) k_shadow<BATCH, 4><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
+    else k_shadow<BATCH, 2><<<Lc.grid_shadow, Lc.block_trace, 0, st>>>(S, P, W, d);
 }
 
 // Orders the live paths of depth d by shade_key into P.qsort.
@@ -1039,6 +1083,14 @@ void enqueue_sort(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Laun
     k_sort_scatter<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
 }
 
+// Orders the live rays of depth d by ray_key into P.qsort.
+void enqueue_raysort(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Launch& Lc, uint32_t d) {
+    cudaStream_t st = ctx->stream;
+    k_raysort_count<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
+    k_sort_scan<<<1, PYRE_SORT_BINS, 0, st>>>(P);
+    k_raysort_scatter<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
+}
+
 void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const WaveParams& W, const Launch& Lc) {
     cudaStream_t st = ctx->stream;
     mark(ctx, STAGE_OTHER);
@@ -1046,6 +1098,7 @@ void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Wave
     k_raygen<false><<<Lc.grid_raygen, Lc.block_stage, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
+        if (W.sort_rays && d > 0) enqueue_raysort(ctx, S, P, Lc, d);
         launch_extend<false>(st, Lc, S, P, W, d);
         mark(ctx, STAGE_SHADE);
         if (W.sort) enqueue_sort(ctx, S, P, Lc, d);
@@ -1070,6 +1123,7 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
     k_raygen<true><<<Lc.grid_raygen, Lc.block_stage, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
+        if (W.sort_rays && d > 0) enqueue_raysort(ctx, S, P, Lc, d);
         launch_extend<true>(st, Lc, S, P, W, d);
         mark(ctx, STAGE_SHADE);
         if (W.sort) enqueue_sort(ctx, S, P, Lc, d);
@@ -1086,7 +1140,8 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
 }
 
 uint32_t kernels_per_wave(const WaveParams& W) {
-    return 4 + W.max_depth * ((W.ns > 0 ? 3 : 2) + (W.sort ? 3 : 0));
+    return 4 + W.max_depth * ((W.ns > 0 ? 3 : 2) + (W.sort ? 3 : 0)) +
+           (W.sort_rays && W.max_depth > 1 ? 3 * (W.max_depth - 1) : 0);
 }
 
 // Largest pixel count of one view: path and pixel indices are 32-bit, and a
@@ -1187,6 +1242,7 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     W.refill = refill_lanes(&rp);
     W.refill_any = refill_lanes(&rp, true);
     W.sort = rp.sort_by_material ? 1 : 0;
+    W.sort_rays = PYRE_SORT_RAYS;
     W.prog_mean = prog;
     DevScene D;
     rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width);
@@ -1209,7 +1265,7 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     S.keep_L = keep;
     if (film->mem == PYRE_MEM_HOST && (rc = ensure_workspace(ctx, ctx->io_ws, film_bytes))) return rc;
 
-    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width, trace_smem(D));
+    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
 
     cudaStream_t st = ctx->stream;
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_r, 0, (size_t)W.npix * sizeof(float4), st));
@@ -1344,6 +1400,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     cap = std::min<uint64_t>(std::max<uint64_t>(cap, max_npix), (uint64_t)1 << 31);
     std::vector<DevSeg> segs;
     std::vector<DevWave> waves;
+    std::vector<uint32_t> last_wave(n_jobs, 0);  // the wave that completes each job
     DevWave cur{0, 0, 0, 0};
     for (uint32_t j = 0; j < n_jobs; ++j) {
         uint32_t s = jobs[j].spp_begin, remaining = jobs[j].spp_end - jobs[j].spp_begin;
@@ -1354,6 +1411,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
                 cur = DevWave{(uint32_t)segs.size(), 0, 0, 0};
                 continue;
             }
+            last_wave[j] = (uint32_t)waves.size();
             segs.push_back(DevSeg{j, s, (uint32_t)k, cur.n_paths, cur.n_slots});
             cur.seg_count += 1;
             cur.n_paths += (uint32_t)(k * dj[j].npix);
@@ -1373,6 +1431,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     W.refill = refill_lanes(params);
     W.refill_any = refill_lanes(params, true);
     W.sort = params && params->sort_by_material ? 1 : 0;
+    W.sort_rays = PYRE_SORT_RAYS;
     DevScene D;
     int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), params ? params->bvh_width : 0u, &D, &W.bvh_width);
     if (rc) return rc;
@@ -1405,52 +1464,82 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.acc_n, 0, total_pix * sizeof(float4), st));
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
 
-    const Launch Lc = make_launch<true>(ctx, params ? params->block_size : 0u, W.bvh_width, trace_smem(D));
+    const Launch Lc = make_launch<true>(ctx, params ? params->block_size : 0u, W.bvh_width);
+
+    const uint32_t n_waves = (uint32_t)waves.size();
+    // Jobs completed by each wave: [done_lo[w], done_lo[w + 1]) (jobs are packed in order, so their last
+    // waves do not decrease).
+    std::vector<uint32_t> done_lo(n_waves + 1, n_jobs);
+    for (uint32_t j = n_jobs; j-- > 0;) done_lo[last_wave[j]] = j;
+    for (uint32_t w = n_waves; w-- > 0;) done_lo[w] = std::min(done_lo[w], done_lo[w + 1]);
+    if (!ctx->copy_stream)
+        PYRE_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    while (ctx->wave_ev.size() < n_waves) {
+        cudaEvent_t e;
+        PYRE_CUDA_TRY(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->wave_ev.push_back(e);
+    }
 
     PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], st));
     ctx->stage_used = 0;
-    const uint32_t n_waves = (uint32_t)waves.size();
     if (use_graph) {
-        // The whole batch (every wave) as one graph, launched once.
-        std::string key = "batch/" + std::to_string(scene->serial) + "/" +
-                          std::to_string((uintptr_t)ctx->render_ws.ptr) + "/" + std::to_string(n_waves) + "/" +
-                          std::to_string(max_depth) + "/" + std::to_string(max_paths) + "/b" +
+        // One wave (its bounce loop) as a graph: every wave runs the same kernels, and the kernels read which
+        // segments the current wave holds from the device tables (WaveCtl::wave), so the graph is replayed
+        // once per wave.
+        std::string key = "batchwave/" + std::to_string(scene->serial) + "/" +
+                          std::to_string((uintptr_t)ctx->render_ws.ptr) + "/" + std::to_string(max_depth) + "/" +
+                          std::to_string(max_paths) + "/" + std::to_string(total_pix) + "/" +
+                          std::to_string(dj.size()) + "/" + std::to_string(segs.size()) + "/b" +
                           std::to_string(Lc.block_stage) + "x" + std::to_string(Lc.block_shade) + "x" +
-                          std::to_string(Lc.block_trace) + "/r" +
-                          std::to_string(W.refill) + "/s" + std::to_string(W.sort) + "/w" + std::to_string(W.bvh_width) +
-                          "/";
-        key.append(reinterpret_cast<const char*>(dj.data()), job_bytes);
+                          std::to_string(Lc.block_trace) + "/r" + std::to_string(W.refill) + "/s" +
+                          std::to_string(W.sort) + "/w" + std::to_string(W.bvh_width);
         if (!ctx->wave_graph || ctx->wave_graph_key != key) {
             if (ctx->wave_graph) { cudaGraphExecDestroy(ctx->wave_graph); ctx->wave_graph = nullptr; }
             cudaGraph_t g;
             PYRE_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            for (uint32_t w = 0; w < n_waves; ++w) enqueue_wave_batch(ctx, D, S, W, Lc);
+            enqueue_wave_batch(ctx, D, S, W, Lc);
             PYRE_CUDA_TRY(ctx, cudaStreamEndCapture(st, &g));
             cudaError_t e = cudaGraphInstantiate(&ctx->wave_graph, g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) { ctx->wave_graph = nullptr; return cuda_check(ctx, e, "cudaGraphInstantiate"); }
             ctx->wave_graph_key = key;
         }
-        PYRE_CUDA_TRY(ctx, cudaGraphLaunch(ctx->wave_graph, st));
-    } else {
-        for (uint32_t w = 0; w < n_waves; ++w) enqueue_wave_batch(ctx, D, S, W, Lc);
     }
-    PYRE_CUDA_TRY(ctx, cudaGetLastError());
-    k_finalize_batch<<<Lc.grid_acc, 256, 0, st>>>(S, d_jobs, n_jobs, (uint32_t)total_pix, d_stage);
-    PYRE_CUDA_TRY(ctx, cudaGetLastError());
-    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[1], st));
-    for (uint32_t j = 0; j < n_jobs; ++j) {
-        const pyre_film& f = jobs[j].film;
-        const cudaMemcpyKind kind = f.mem == PYRE_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-        const size_t a = dj[j].acc_base, n = dj[j].npix;
-        float* outs[4] = {f.radiance, f.albedo, f.normal, f.depth};
-        for (int c = 0; c < 4; ++c) {
-            if (!outs[c]) continue;
-            const size_t comps = c == 3 ? 1 : 3;
-            const float* src = d_stage + (size_t)c * 3 * total_pix + comps * a;
-            PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(outs[c], src, comps * n * sizeof(float), kind, st));
+    // Every wave is enqueued first; after the wave that completes some jobs, their films are finalized and
+    // an event marks them done. The copies to the callers' films then run on a second stream while the GPU
+    // renders the waves that follow, which per-view calls (one synchronous render each) cannot overlap.
+    uint32_t finalizes = 0;
+    for (uint32_t w = 0; w < n_waves; ++w) {
+        if (use_graph) PYRE_CUDA_TRY(ctx, cudaGraphLaunch(ctx->wave_graph, st));
+        else enqueue_wave_batch(ctx, D, S, W, Lc);
+        const uint32_t j0 = done_lo[w], j1 = done_lo[w + 1];
+        if (j0 < j1) {
+            const uint32_t a0 = dj[j0].acc_base, a1 = dj[j1 - 1].acc_base + dj[j1 - 1].npix;
+            k_finalize_batch<<<Lc.grid_acc, 256, 0, st>>>(S, d_jobs, n_jobs, (uint32_t)total_pix, a0, a1, d_stage);
+            ++finalizes;
+            PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->wave_ev[w], st));
         }
     }
+    PYRE_CUDA_TRY(ctx, cudaGetLastError());
+    PYRE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[1], st));
+    cudaStream_t cst = ctx->copy_stream;
+    for (uint32_t w = 0; w < n_waves; ++w) {
+        if (done_lo[w] == done_lo[w + 1]) continue;
+        PYRE_CUDA_TRY(ctx, cudaStreamWaitEvent(cst, ctx->wave_ev[w], 0));
+        for (uint32_t j = done_lo[w]; j < done_lo[w + 1]; ++j) {
+            const pyre_film& f = jobs[j].film;
+            const cudaMemcpyKind kind = f.mem == PYRE_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+            const size_t a = dj[j].acc_base, n = dj[j].npix;
+            float* outs[4] = {f.radiance, f.albedo, f.normal, f.depth};
+            for (int c = 0; c < 4; ++c) {
+                if (!outs[c]) continue;
+                const size_t comps = c == 3 ? 1 : 3;
+                const float* src = d_stage + (size_t)c * 3 * total_pix + comps * a;
+                PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(outs[c], src, comps * n * sizeof(float), kind, cst));
+            }
+        }
+    }
+    PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(cst));
     WaveCtl ctl;
     PYRE_CUDA_TRY(ctx, cudaMemcpyAsync(&ctl, S.ctl, sizeof ctl, cudaMemcpyDeviceToHost, st));
     PYRE_CUDA_TRY(ctx, cudaStreamSynchronize(st));
@@ -1461,7 +1550,7 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     s.extend_rays = ctl.extend_rays;
     s.shadow_rays = ctl.shadow_rays;
     s.waves = n_waves;
-    s.kernel_launches = n_waves * kernels_per_wave(W) + 1;
+    s.kernel_launches = n_waves * kernels_per_wave(W) + finalizes;
     cudaEventElapsedTime(&s.ms_total, ctx->ev[0], ctx->ev[1]);
     return PYRE_OK;
 }
@@ -1522,6 +1611,7 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     W.refill = refill_lanes(&rp);
     W.refill_any = refill_lanes(&rp, true);
     W.sort = rp.sort_by_material ? 1 : 0;
+    W.sort_rays = PYRE_SORT_RAYS;
     DevScene D;
     rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width, false);
     if (rc) return rc;
@@ -1559,7 +1649,7 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     PathSoA S;
     carve_paths((char*)scratch, (size_t)W.npix * K, ns, W.npix, &S);
 
-    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width, trace_smem(D));
+    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
 
     cudaStream_t st = ctx->stream;
     // The array keeps the previous call's contents: clear the sums and counters.
@@ -1596,16 +1686,12 @@ template <bool ANY>
 static void launch_intersect(pyre_ctx* ctx, const DevScene& D, const QueryRays& q, uint32_t n, int width) {
     cudaStream_t st = ctx->stream;
     const int refill = ANY ? PYRE_DEFAULT_REFILL_ANY : PYRE_DEFAULT_REFILL;
-    const size_t sm = trace_smem(D);
     if (width == 8) {
-        k_intersect<ANY, 8><<<grid_for(ctx, k_intersect<ANY, 8>, 128, sm), 128, sm, st>>>(D, q, n, ctx->d_counter,
-                                                                                          refill);
+        k_intersect<ANY, 8><<<grid_for(ctx, k_intersect<ANY, 8>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter, refill);
     } else if (width == 4) {
-        k_intersect<ANY, 4><<<grid_for(ctx, k_intersect<ANY, 4>, 128, sm), 128, sm, st>>>(D, q, n, ctx->d_counter,
-                                                                                          refill);
+        k_intersect<ANY, 4><<<grid_for(ctx, k_intersect<ANY, 4>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter, refill);
     } else {
-        k_intersect<ANY, 2><<<grid_for(ctx, k_intersect<ANY, 2>, 128, sm), 128, sm, st>>>(D, q, n, ctx->d_counter,
-                                                                                          refill);
+        k_intersect<ANY, 2><<<grid_for(ctx, k_intersect<ANY, 2>, 128), 128, 0, st>>>(D, q, n, ctx->d_counter, refill);
     }
 }
 
@@ -1788,6 +1874,7 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     W.refill = refill_lanes(&rp);
     W.refill_any = refill_lanes(&rp, true);
     W.sort = rp.sort_by_material ? 1 : 0;
+    W.sort_rays = PYRE_SORT_RAYS;
     DevScene D;
     if ((rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width))) return rc;
     const uint32_t spp = rp.spp_end - rp.spp_begin;
@@ -1830,7 +1917,7 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     const size_t smem = mat_bytes <= 48 * 1024 ? mat_bytes : 0;
     W.smem_grad = smem ? 1 : 0;
 
-    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width, trace_smem(D));
+    const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
     const int grid_adj = grid_for(ctx, k_shade<false, true>, Lc.block_stage, smem);
     const int grid_acc = grid_for(ctx, k_accumulate_adjoint, Lc.block_stage, smem);
     PYRE_CUDA_TRY(ctx, cudaMemsetAsync(S.ctl, 0, sizeof(WaveCtl), st));
@@ -1839,6 +1926,7 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
         k_wave_begin<<<1, 32, 0, st>>>(S.ctl, W.spp_begin, W.spp_end, W.k_per_wave, W.npix);
         k_raygen<false><<<Lc.grid_raygen, Lc.block_stage, 0, st>>>(S, W);
         for (uint32_t d = 0; d < W.max_depth; ++d) {
+            if (W.sort_rays && d > 0) enqueue_raysort(ctx, D, S, Lc, d);
             launch_extend<false>(st, Lc, D, S, W, d);
             if (W.sort) enqueue_sort(ctx, D, S, Lc, d);
             k_shade<false, true><<<grid_adj, Lc.block_stage, smem, st>>>(D, S, W, d);

@@ -60,6 +60,10 @@ struct pyre_ctx {
     // CUDA graph of one wave, keyed by the render configuration it was captured for.
     cudaGraphExec_t wave_graph = nullptr;
     std::string wave_graph_key;
+    // pyre_render_batch: films of finished jobs are copied on this stream while later waves render; one
+    // event per wave marks the jobs it completes
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> wave_ev;
 };
 
 namespace pyre {
