@@ -327,6 +327,8 @@ def extra_batch(reps: int = 1) -> dict:
         ctx.render_batch(ds, spec, use_graph=1, films=films)
         return time.perf_counter() - t0, ctx.stats().ms_total / 1e3
 
+    per_job = {}
+
     def per_view(small_only=False):
         wall = dev = 0.0
         n = 0
@@ -335,15 +337,30 @@ def extra_batch(reps: int = 1) -> dict:
                 continue
             t0 = time.perf_counter()
             ctx.render_into(ds1, j["camera"], params[k], cfilms[k])
-            wall += time.perf_counter() - t0
-            dev += ctx.stats().ms_total / 1e3
+            w1 = time.perf_counter() - t0
+            d1 = ctx.stats().ms_total / 1e3
+            wall += w1
+            dev += d1
             n += j["width"] * j["height"] * j["spp"]
+            per_job[k] = (w1, d1)
         return wall, dev, n
 
     batched()
     b = sorted(batched() for _ in range(reps))[reps // 2]
     per_view()
     v = sorted(per_view()[:2] for _ in range(reps))[reps // 2]
+    # per-view cost by image size: where the samples and the time are
+    by_size = {}
+    for k, j in enumerate(jobs):
+        e = by_size.setdefault(f"{j['width']}^2", {"jobs": 0, "samples": 0, "per_view_e2e_ms": 0.0,
+                                                   "per_view_device_ms": 0.0})
+        e["jobs"] += 1
+        e["samples"] += j["width"] * j["height"] * j["spp"]
+        e["per_view_e2e_ms"] += 1e3 * per_job[k][0]
+        e["per_view_device_ms"] += 1e3 * per_job[k][1]
+    for e in by_size.values():
+        e["per_view_device_msamples_per_s"] = e["samples"] / e["per_view_device_ms"] / 1e3
+        e["per_view_e2e_msamples_per_s"] = e["samples"] / e["per_view_e2e_ms"] / 1e3
     # the small views alone (128^2 and 256^2), where launch and host gaps weigh most
     small_idx = [k for k, j in enumerate(jobs) if j["width"] <= 256]
     sub = CudaIntegrator(0)
@@ -367,6 +384,7 @@ def extra_batch(reps: int = 1) -> dict:
             "batched_e2e_msamples_per_s": samples / b[0] / 1e6, "batched_device_msamples_per_s": samples / b[1] / 1e6,
             "per_view_e2e_msamples_per_s": samples / v[0] / 1e6, "per_view_device_msamples_per_s": samples / v[1] / 1e6,
             "batched_over_per_view_e2e": v[0] / b[0], "batched_over_per_view_device": v[1] / b[1],
+            "per_view_by_size": dict(sorted(by_size.items(), key=lambda kv: int(kv[0].split("^")[0]))),
             "small_jobs": {"jobs": len(small_idx), "samples": s_samples,
                            "batched_over_per_view_e2e": sv_wall / sb_wall,
                            "batched_over_per_view_device": sv_dev / sb_dev}}

@@ -478,9 +478,6 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     // ---- instances and one top-level BVH per part over their swept bounds
     std::vector<DevInstance> inst;
     std::vector<int32_t> part_tlas(n_parts, -1);
-    Aabb world;  // union of the instances' swept bounds
-    world.lo = splat3(std::numeric_limits<float>::infinity());
-    world.hi = splat3(-std::numeric_limits<float>::infinity());
     sc->slot_of_instance.assign(desc->n_instances, -1);
     for (uint32_t part = 0; part < n_parts; ++part) {
         std::vector<uint32_t> live;  // instances of this part with geometry
@@ -510,8 +507,6 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
             w.hi = w.hi + splat3(pad);
             live.push_back(i);
             ibox.push_back(w);
-            world.lo = vmin3(world.lo, w.lo);
-            world.hi = vmax3(world.hi, w.hi);
             icent.push_back((w.lo + w.hi) * 0.5f);
         }
         if (live.empty()) continue;
@@ -613,15 +608,6 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     D.inst = d_inst;
     D.n_inst = (uint32_t)inst.size();
     D.tlas_root = tlas_root;
-    {
-        const float lo[3] = {world.lo.x, world.lo.y, world.lo.z}, hi[3] = {world.hi.x, world.hi.y, world.hi.z};
-        const float cells[3] = {8.0f, 4.0f, 4.0f};
-        for (int k = 0; k < 3; ++k) {
-            const bool ok = hi[k] > lo[k];
-            D.cell_lo[k] = ok ? lo[k] : 0.0f;
-            D.cell_scale[k] = ok ? cells[k] / (hi[k] - lo[k]) : 0.0f;
-        }
-    }
     uint32_t* d_index = nullptr;
     if ((rc = upload(ctx, sc, index, &d_index)) != PYRE_OK) return fail(rc);
     D.index = d_index;

@@ -84,11 +84,7 @@ struct DevScene {
     // root of each instance slot
     const float4* wnodes;
     const int32_t* wroot;
-    // the instances' (swept) world bounds, for the coarse spatial key of the ray reordering:
-    // cell = (o - cell_lo) * cell_scale, 8 x 4 x 4 cells
-    float cell_lo[3], cell_scale[3];
 };
-
 
 struct TraceRay {
     f3 o, d;

@@ -32,9 +32,6 @@ namespace cg = cooperative_groups;
 namespace pyre {
 
 #define PYRE_MAX_DEPTH 64
-#ifndef PYRE_SORT_RAYS
-#define PYRE_SORT_RAYS 0  // extend traces the rays of depth >= 1 grouped by ray_key
-#endif
 #define PYRE_SORT_BINS 1024  // shade-queue sort keys: escaped, light hit, then materials
 
 struct WaveCtl {
@@ -95,7 +92,6 @@ struct WaveParams {
     int refill_any;      // the same for the any-hit (shadow) traversal
     int sort;            // shade reads the live paths sorted by material (P.qsort)
     int bvh_width;       // instance BVH width of the traversal kernels: 2, 4 or 8
-    int sort_rays;       // extend reads the live rays of depth >= 1 grouped by (origin cell, direction octant)
     // progressive accumulation (pyre_render_progressive): crop npix x 3 running
     // mean of the radiance, updated once per sample in sample order
     float* prog_mean;
@@ -304,11 +300,9 @@ struct ExtendRays {
     const WaveParams* W;
     const uint32_t* qin;  // live-path queue; null at depth 0 (every path of the wave)
     uint32_t depth;
-    const uint32_t* order;  // queue positions grouped by ray key (reordered rays), or null
-    // ray j of the queue sits at queue position j (depth 0: path tiled_path(j)); with `order` the j-th ray
-    // traced is the one at queue position order[j], and its hit goes back to that position
+    // ray j of the queue sits at queue position j (depth 0: path tiled_path(j))
     __device__ __forceinline__ uint32_t load(uint32_t j, TraceRay& r, int32_t& root) const {
-        const uint32_t p = order ? __ldcs(order + j) : qin ? j : (BATCH ? j : tiled_path(*W, j));
+        const uint32_t p = qin ? j : (BATCH ? j : tiled_path(*W, j));
         const float4 ro = __ldcs(P->ray_o[depth & 1] + p), rd = __ldcs(P->ray_d[depth & 1] + p);
         r.o = mk3(ro.x, ro.y, ro.z);
         r.d = mk3(rd.x, rd.y, rd.z);
@@ -337,8 +331,7 @@ struct ExtendRays {
 // unconstrained 70-register build by 2 %; 10 blocks (48 registers) lose 2 %.
 template <bool BATCH, int WIDTH>
 __global__ void __launch_bounds__(128, 9) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
-    ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1], depth,
-                          (W.sort_rays && depth > 0) ? P.qsort : nullptr};
+    ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1], depth};
     trace_stream<false, WIDTH>(S, src, P.ctl->count[depth], &P.ctl->fetch[2 * depth], W.refill);
 }
 
@@ -463,46 +456,6 @@ __global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
         if (lane == leader) base = atomicAdd(&P.ctl->sort_off[key], (uint32_t)__popc(peers));
         base = __shfl_sync(peers, base, leader);
         P.qsort[base + __popc(peers & below)] = j;  // the queue position
-    }
-}
-
-// -------------------------------------------------------- ray reordering --
-// Extend at depth >= 1 can trace the live rays grouped by a coarse key: the
-// cell of the origin in an 8 x 4 x 4 grid over the instances' bounds, then
-// the direction's octant (1024 keys). A counting sort gives the order; within
-// a key the rays keep roughly their queue order, which follows the pixels, so
-// a warp gets rays from nearby origins heading the same way. Hits go back to
-// the rays' own queue positions, so shade and the results do not change.
-__device__ __forceinline__ uint32_t ray_key(const DevScene& S, const float4& o, const float4& d) {
-    const int cx = min(max((int)((o.x - S.cell_lo[0]) * S.cell_scale[0]), 0), 7);
-    const int cy = min(max((int)((o.y - S.cell_lo[1]) * S.cell_scale[1]), 0), 3);
-    const int cz = min(max((int)((o.z - S.cell_lo[2]) * S.cell_scale[2]), 0), 3);
-    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-    return ((uint32_t)(cx << 4 | cy << 2 | cz) << 3) | oct;
-}
-
-__global__ void k_raysort_count(DevScene S, PathSoA P, uint32_t depth) {
-    const uint32_t n = P.ctl->count[depth];
-    const int lane = threadIdx.x & 31;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t key = ray_key(S, P.ray_o[depth & 1][j], P.ray_d[depth & 1][j]);
-        const unsigned peers = __match_any_sync(__activemask(), key);
-        if (lane == __ffs(peers) - 1) atomicAdd(&P.ctl->sort_hist[key], (uint32_t)__popc(peers));
-    }
-}
-
-__global__ void k_raysort_scatter(DevScene S, PathSoA P, uint32_t depth) {
-    const uint32_t n = P.ctl->count[depth];
-    const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t key = ray_key(S, P.ray_o[depth & 1][j], P.ray_d[depth & 1][j]);
-        const unsigned peers = __match_any_sync(__activemask(), key);
-        const int leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&P.ctl->sort_off[key], (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader);
-        P.qsort[base + __popc(peers & below)] = j;
     }
 }
 
@@ -1083,14 +1036,6 @@ void enqueue_sort(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Laun
     k_sort_scatter<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
 }
 
-// Orders the live rays of depth d by ray_key into P.qsort.
-void enqueue_raysort(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Launch& Lc, uint32_t d) {
-    cudaStream_t st = ctx->stream;
-    k_raysort_count<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
-    k_sort_scan<<<1, PYRE_SORT_BINS, 0, st>>>(P);
-    k_raysort_scatter<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
-}
-
 void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const WaveParams& W, const Launch& Lc) {
     cudaStream_t st = ctx->stream;
     mark(ctx, STAGE_OTHER);
@@ -1098,7 +1043,6 @@ void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Wave
     k_raygen<false><<<Lc.grid_raygen, Lc.block_stage, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
-        if (W.sort_rays && d > 0) enqueue_raysort(ctx, S, P, Lc, d);
         launch_extend<false>(st, Lc, S, P, W, d);
         mark(ctx, STAGE_SHADE);
         if (W.sort) enqueue_sort(ctx, S, P, Lc, d);
@@ -1123,7 +1067,6 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
     k_raygen<true><<<Lc.grid_raygen, Lc.block_stage, 0, st>>>(P, W);
     for (uint32_t d = 0; d < W.max_depth; ++d) {
         mark(ctx, STAGE_EXTEND);
-        if (W.sort_rays && d > 0) enqueue_raysort(ctx, S, P, Lc, d);
         launch_extend<true>(st, Lc, S, P, W, d);
         mark(ctx, STAGE_SHADE);
         if (W.sort) enqueue_sort(ctx, S, P, Lc, d);
@@ -1140,8 +1083,7 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
 }
 
 uint32_t kernels_per_wave(const WaveParams& W) {
-    return 4 + W.max_depth * ((W.ns > 0 ? 3 : 2) + (W.sort ? 3 : 0)) +
-           (W.sort_rays && W.max_depth > 1 ? 3 * (W.max_depth - 1) : 0);
+    return 4 + W.max_depth * ((W.ns > 0 ? 3 : 2) + (W.sort ? 3 : 0));
 }
 
 // Largest pixel count of one view: path and pixel indices are 32-bit, and a
@@ -1242,7 +1184,6 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     W.refill = refill_lanes(&rp);
     W.refill_any = refill_lanes(&rp, true);
     W.sort = rp.sort_by_material ? 1 : 0;
-    W.sort_rays = PYRE_SORT_RAYS;
     W.prog_mean = prog;
     DevScene D;
     rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width);
@@ -1431,7 +1372,6 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     W.refill = refill_lanes(params);
     W.refill_any = refill_lanes(params, true);
     W.sort = params && params->sort_by_material ? 1 : 0;
-    W.sort_rays = PYRE_SORT_RAYS;
     DevScene D;
     int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), params ? params->bvh_width : 0u, &D, &W.bvh_width);
     if (rc) return rc;
@@ -1611,7 +1551,6 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     W.refill = refill_lanes(&rp);
     W.refill_any = refill_lanes(&rp, true);
     W.sort = rp.sort_by_material ? 1 : 0;
-    W.sort_rays = PYRE_SORT_RAYS;
     DevScene D;
     rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width, false);
     if (rc) return rc;
@@ -1874,7 +1813,6 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     W.refill = refill_lanes(&rp);
     W.refill_any = refill_lanes(&rp, true);
     W.sort = rp.sort_by_material ? 1 : 0;
-    W.sort_rays = PYRE_SORT_RAYS;
     DevScene D;
     if ((rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width))) return rc;
     const uint32_t spp = rp.spp_end - rp.spp_begin;
@@ -1926,7 +1864,6 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
         k_wave_begin<<<1, 32, 0, st>>>(S.ctl, W.spp_begin, W.spp_end, W.k_per_wave, W.npix);
         k_raygen<false><<<Lc.grid_raygen, Lc.block_stage, 0, st>>>(S, W);
         for (uint32_t d = 0; d < W.max_depth; ++d) {
-            if (W.sort_rays && d > 0) enqueue_raysort(ctx, D, S, Lc, d);
             launch_extend<false>(st, Lc, D, S, W, d);
             if (W.sort) enqueue_sort(ctx, D, S, Lc, d);
             k_shade<false, true><<<grid_adj, Lc.block_stage, smem, st>>>(D, S, W, d);
