@@ -103,6 +103,9 @@ struct TraceHit {
 // starts, for closest-hit and any-hit traversal
 #define PYRE_LEAF_WAIT_CLOSEST 8
 #define PYRE_LEAF_WAIT_ANY 12
+#ifndef PYRE_STEPS_PER_VOTE
+#define PYRE_STEPS_PER_VOTE 1  // node steps a lane takes between two warp votes of the inner phase
+#endif
 
 // Rust-order slab test (bvh.rs:146-153): t1/t2 per axis, max of mins vs
 // t_min, min of maxes vs t_max, hit iff tmin <= tmax. Returns the entry.
@@ -305,117 +308,121 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
             const int seeking = __popc(__ballot_sync(FULL, active && !exhausted && !hit_any && parked == 0));
             if (seeking == 0) break;
             if (seeking <= LEAF_WAIT && __any_sync(FULL, active && !hit_any && parked > 0)) break;
-            if (!active || exhausted || hit_any || parked >= STOP) continue;
-            if (node == PYRE_NODE_NONE) {
-                if (sp == 0) { exhausted = true; continue; }
-                node = spop();
-            }
-            if (node == PYRE_NODE_EXIT) {
-                if (parked) { spush(PYRE_NODE_EXIT); node = PYRE_NODE_NONE; parked = STOP; continue; }
-                inst = -1;
-                o = r.o;
-                node = PYRE_NODE_NONE;
-                continue;
-            }
-            if (node & PYRE_TAG_INST) {
-                if (parked) { spush(node); node = PYRE_NODE_NONE; parked = STOP; continue; }
-                const int k = node & ~PYRE_TAG_INST;
-                node = PYRE_NODE_NONE;
-                const DevInstance& I = S.inst[k];
-                const int root = WIDTH > 2 ? S.wroot[k] : I.blas_root;
-                if (root < 0) continue;
-                f3 lo = r.o;
-                if (I.has_motion) {
-                    f3 off = motion_offset(I, r.time);
-                    if (!is_zero3(off)) lo = r.o - off;
+            // each lane takes up to PYRE_STEPS_PER_VOTE node steps between the warp's votes
+#pragma unroll 1
+            for (int step = 0; step < PYRE_STEPS_PER_VOTE; ++step) {
+                if (!active || exhausted || hit_any || parked >= STOP) break;
+                if (node == PYRE_NODE_NONE) {
+                    if (sp == 0) { exhausted = true; continue; }
+                    node = spop();
                 }
-                float e;
-                if (!slab(I.lo[0], I.hi[0], I.lo[1], I.hi[1], I.lo[2], I.hi[2], lo, inv, r.tmin, best_t, &e)) continue;
-                if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
-                spush(PYRE_NODE_EXIT);
-                inst = k;
-                o = lo;
-                node = root;
-                continue;
-            }
-            const bool top = (node & PYRE_TAG_TOP) != 0;
-            if (WIDTH > 2 && !top) {
-                if (node & PYRE_TAG_LEAF) {  // park a leaf child of a wide node
-                    const uint32_t ref = (uint32_t)(node & ~PYRE_TAG_LEAF);
-                    const int32_t* NI = reinterpret_cast<const int32_t*>(S.wnodes) +
-                                        (size_t)(ref / WIDTH) * (PYRE_WIDE_FIELDS * WIDTH) + ref % WIDTH;
-                    ls[parked] = __ldg(NI + 6 * WIDTH);
-                    lc[parked] = __ldg(NI + 7 * WIDTH);
-                    ++parked;
+                if (node == PYRE_NODE_EXIT) {
+                    if (parked) { spush(PYRE_NODE_EXIT); node = PYRE_NODE_NONE; parked = STOP; continue; }
+                    inst = -1;
+                    o = r.o;
                     node = PYRE_NODE_NONE;
                     continue;
                 }
-                constexpr int Q = WIDTH / 4;  // float4 rows per field
-                const float4* N = S.wnodes + (size_t)node * (2 * WIDTH);
-                float e[WIDTH];
-                int ent[WIDTH];
-#pragma unroll
-                for (int q = 0; q < Q; ++q) {
-                    const float4 lx = __ldg(N + 0 * Q + q), hx = __ldg(N + 1 * Q + q), ly = __ldg(N + 2 * Q + q),
-                                 hy = __ldg(N + 3 * Q + q), lz = __ldg(N + 4 * Q + q), hz = __ldg(N + 5 * Q + q);
-                    const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6 * Q + q));
-                    const int4 ct = __ldg(reinterpret_cast<const int4*>(N + 7 * Q + q));
-                    const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
-                    const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
-                    const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
-                    const int CH[4] = {ch.x, ch.y, ch.z, ch.w}, CT[4] = {ct.x, ct.y, ct.z, ct.w};
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        float ek;
-                        const bool h = CH[k] >= 0 && slab(LX[k], HX[k], LY[k], HY[k], LZ[k], HZ[k], o, inv, r.tmin,
-                                                          best_t, &ek);
-                        e[4 * q + k] = h ? ek : __int_as_float(0x7f800000);
-                        ent[4 * q + k] = !h ? PYRE_NODE_NONE
-                                            : (CT[k] > 0 ? (PYRE_TAG_LEAF | (node * WIDTH + 4 * q + k)) : CH[k]);
+                if (node & PYRE_TAG_INST) {
+                    if (parked) { spush(node); node = PYRE_NODE_NONE; parked = STOP; continue; }
+                    const int k = node & ~PYRE_TAG_INST;
+                    node = PYRE_NODE_NONE;
+                    const DevInstance& I = S.inst[k];
+                    const int root = WIDTH > 2 ? S.wroot[k] : I.blas_root;
+                    if (root < 0) continue;
+                    f3 lo = r.o;
+                    if (I.has_motion) {
+                        f3 off = motion_offset(I, r.time);
+                        if (!is_zero3(off)) lo = r.o - off;
                     }
+                    float e;
+                    if (!slab(I.lo[0], I.hi[0], I.lo[1], I.hi[1], I.lo[2], I.hi[2], lo, inv, r.tmin, best_t, &e)) continue;
+                    if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
+                    spush(PYRE_NODE_EXIT);
+                    inst = k;
+                    o = lo;
+                    node = root;
+                    continue;
                 }
-                sort_children<WIDTH>(e, ent);
-                int nh = 0;
-#pragma unroll
-                for (int k = 1; k < WIDTH; ++k) nh += ent[k] != PYRE_NODE_NONE ? 1 : 0;
-                if (sp + nh > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
-#pragma unroll
-                for (int k = WIDTH - 1; k >= 1; --k)
-                    if (ent[k] != PYRE_NODE_NONE) spush(ent[k]);
-                node = ent[0];
-                continue;
-            }
-            const float4* N = S.nodes + 4 * (size_t)(node & ~PYRE_TAG_TOP);
-            const float4 na = __ldg(N), nb = __ldg(N + 1), nc = __ldg(N + 2);
-            const int4 nd = __ldg(reinterpret_cast<const int4*>(N + 3));
-            float e0, e1;
-            const bool h0 = nd.x >= 0 && slab(na.x, na.y, na.z, na.w, nc.x, nc.y, o, inv, r.tmin, best_t, &e0);
-            const bool h1 = nd.y >= 0 && slab(nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, o, inv, r.tmin, best_t, &e1);
-            node = PYRE_NODE_NONE;
-            const bool leaf0 = nd.z > 0, leaf1 = nd.w > 0;
-            // leaves: park triangle ranges, or queue the instances of a top-level leaf
-            if (top) {
-                const int need = (h0 && leaf0 ? nd.z : 0) + (h1 && leaf1 ? nd.w : 0) + 1;
-                if (sp + need > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
-                if (h1 && leaf1)
-                    for (int k = nd.w - 1; k >= 0; --k) spush(PYRE_TAG_INST | (nd.y + k));
-                if (h0 && leaf0)
-                    for (int k = nd.z - 1; k >= 0; --k) spush(PYRE_TAG_INST | (nd.x + k));
-            } else {
-                if (h0 && leaf0) { ls[parked] = nd.x; lc[parked] = nd.z; ++parked; }
-                if (h1 && leaf1) { ls[parked] = nd.y; lc[parked] = nd.w; ++parked; }
-            }
-            const int tag = top ? PYRE_TAG_TOP : 0;
-            const bool g0 = h0 && !leaf0, g1 = h1 && !leaf1;
-            if (g0 && g1) {
-                const bool first0 = e0 <= e1;
-                if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
-                spush((first0 ? nd.y : nd.x) | tag);
-                node = (first0 ? nd.x : nd.y) | tag;
-            } else if (g0) {
-                node = nd.x | tag;
-            } else if (g1) {
-                node = nd.y | tag;
+                const bool top = (node & PYRE_TAG_TOP) != 0;
+                if (WIDTH > 2 && !top) {
+                    if (node & PYRE_TAG_LEAF) {  // park a leaf child of a wide node
+                        const uint32_t ref = (uint32_t)(node & ~PYRE_TAG_LEAF);
+                        const int32_t* NI = reinterpret_cast<const int32_t*>(S.wnodes) +
+                                            (size_t)(ref / WIDTH) * (PYRE_WIDE_FIELDS * WIDTH) + ref % WIDTH;
+                        ls[parked] = __ldg(NI + 6 * WIDTH);
+                        lc[parked] = __ldg(NI + 7 * WIDTH);
+                        ++parked;
+                        node = PYRE_NODE_NONE;
+                        continue;
+                    }
+                    constexpr int Q = WIDTH / 4;  // float4 rows per field
+                    const float4* N = S.wnodes + (size_t)node * (2 * WIDTH);
+                    float e[WIDTH];
+                    int ent[WIDTH];
+    #pragma unroll
+                    for (int q = 0; q < Q; ++q) {
+                        const float4 lx = __ldg(N + 0 * Q + q), hx = __ldg(N + 1 * Q + q), ly = __ldg(N + 2 * Q + q),
+                                     hy = __ldg(N + 3 * Q + q), lz = __ldg(N + 4 * Q + q), hz = __ldg(N + 5 * Q + q);
+                        const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6 * Q + q));
+                        const int4 ct = __ldg(reinterpret_cast<const int4*>(N + 7 * Q + q));
+                        const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
+                        const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
+                        const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
+                        const int CH[4] = {ch.x, ch.y, ch.z, ch.w}, CT[4] = {ct.x, ct.y, ct.z, ct.w};
+    #pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            float ek;
+                            const bool h = CH[k] >= 0 && slab(LX[k], HX[k], LY[k], HY[k], LZ[k], HZ[k], o, inv, r.tmin,
+                                                              best_t, &ek);
+                            e[4 * q + k] = h ? ek : __int_as_float(0x7f800000);
+                            ent[4 * q + k] = !h ? PYRE_NODE_NONE
+                                                : (CT[k] > 0 ? (PYRE_TAG_LEAF | (node * WIDTH + 4 * q + k)) : CH[k]);
+                        }
+                    }
+                    sort_children<WIDTH>(e, ent);
+                    int nh = 0;
+    #pragma unroll
+                    for (int k = 1; k < WIDTH; ++k) nh += ent[k] != PYRE_NODE_NONE ? 1 : 0;
+                    if (sp + nh > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
+    #pragma unroll
+                    for (int k = WIDTH - 1; k >= 1; --k)
+                        if (ent[k] != PYRE_NODE_NONE) spush(ent[k]);
+                    node = ent[0];
+                    continue;
+                }
+                const float4* N = S.nodes + 4 * (size_t)(node & ~PYRE_TAG_TOP);
+                const float4 na = __ldg(N), nb = __ldg(N + 1), nc = __ldg(N + 2);
+                const int4 nd = __ldg(reinterpret_cast<const int4*>(N + 3));
+                float e0, e1;
+                const bool h0 = nd.x >= 0 && slab(na.x, na.y, na.z, na.w, nc.x, nc.y, o, inv, r.tmin, best_t, &e0);
+                const bool h1 = nd.y >= 0 && slab(nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, o, inv, r.tmin, best_t, &e1);
+                node = PYRE_NODE_NONE;
+                const bool leaf0 = nd.z > 0, leaf1 = nd.w > 0;
+                // leaves: park triangle ranges, or queue the instances of a top-level leaf
+                if (top) {
+                    const int need = (h0 && leaf0 ? nd.z : 0) + (h1 && leaf1 ? nd.w : 0) + 1;
+                    if (sp + need > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
+                    if (h1 && leaf1)
+                        for (int k = nd.w - 1; k >= 0; --k) spush(PYRE_TAG_INST | (nd.y + k));
+                    if (h0 && leaf0)
+                        for (int k = nd.z - 1; k >= 0; --k) spush(PYRE_TAG_INST | (nd.x + k));
+                } else {
+                    if (h0 && leaf0) { ls[parked] = nd.x; lc[parked] = nd.z; ++parked; }
+                    if (h1 && leaf1) { ls[parked] = nd.y; lc[parked] = nd.w; ++parked; }
+                }
+                const int tag = top ? PYRE_TAG_TOP : 0;
+                const bool g0 = h0 && !leaf0, g1 = h1 && !leaf1;
+                if (g0 && g1) {
+                    const bool first0 = e0 <= e1;
+                    if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
+                    spush((first0 ? nd.y : nd.x) | tag);
+                    node = (first0 ? nd.x : nd.y) | tag;
+                } else if (g0) {
+                    node = nd.x | tag;
+                } else if (g1) {
+                    node = nd.y | tag;
+                }
             }
         }
         // ---- leaf phase: all lanes test their parked triangles together
