@@ -101,10 +101,19 @@ struct TraceHit {
 #define PYRE_STACK 64
 // lanes of a warp that may still be looking for a leaf when the leaf phase
 // starts, for closest-hit and any-hit traversal
+#ifndef PYRE_LEAF_WAIT_CLOSEST
 #define PYRE_LEAF_WAIT_CLOSEST 8
+#endif
+#ifndef PYRE_LEAF_WAIT_ANY
 #define PYRE_LEAF_WAIT_ANY 12
+#endif
+// Node steps a lane takes between two warp votes of the inner phase. Each
+// vote (a ballot, a population count and an any) costs issue slots; taking
+// two steps per vote measured 701.8 against 681.0 Msamples/s on the 1080p
+// studio frame (extend 104.0 against 109.4 ms), three 700.6. Films are
+// bit-identical for every setting.
 #ifndef PYRE_STEPS_PER_VOTE
-#define PYRE_STEPS_PER_VOTE 1  // node steps a lane takes between two warp votes of the inner phase
+#define PYRE_STEPS_PER_VOTE 2
 #endif
 
 // Rust-order slab test (bvh.rs:146-153): t1/t2 per axis, max of mins vs
