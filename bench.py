@@ -666,6 +666,9 @@ def main():
         tj = json.loads(traffic_file.read_text())
         roofline["traffic"] = tj.get("bytes_per_launch")
         roofline["traffic_note"] = tj.get("note")
+    counters_file = ROOT / "profiles" / "k_extend_counters.json"
+    if counters_file.exists():  # the kernel is issue-bound: these counters say more than the HBM fraction
+        roofline["ncu_counters_bounces_0_1_2"] = json.loads(counters_file.read_text())
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,

@@ -114,14 +114,6 @@ struct TraceHit {
 // two steps per vote measured 701.8 against 681.0 Msamples/s on the 1080p
 // studio frame (extend 104.0 against 109.4 ms), three 700.6. Films are
 // bit-identical for every setting.
-#ifndef PYRE_STACK_TOP_IN_REGISTER
-#define PYRE_STACK_TOP_IN_REGISTER 0
-#endif
-#if PYRE_STACK_TOP_IN_REGISTER
-#define PYRE_DROP_TOP (cached = false)
-#else
-#define PYRE_DROP_TOP ((void)0)
-#endif
 #ifndef PYRE_STEPS_PER_VOTE
 #define PYRE_STEPS_PER_VOTE 2
 #endif
@@ -265,27 +257,6 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
     __shared__ int sstack[SK > 0 ? SK : 1][128];  // traversal blocks have at most 128 threads
     int stack[STACK - SK];
     int sp = 0;
-#if PYRE_STACK_TOP_IN_REGISTER
-    // The top entry stays in a register: a push followed by a pop (push the
-    // far child, and pop it back once the near one is done) touches no memory.
-    int ctop = 0;
-    bool cached = false;
-    auto smem_write = [&](int i, int v) {
-        if (SK > 0 && i < SK) sstack[i][threadIdx.x] = v;
-        else stack[i - SK] = v;
-    };
-    auto spush = [&](int v) {
-        if (cached) smem_write(sp - 1, ctop);
-        ctop = v;
-        cached = true;
-        ++sp;
-    };
-    auto spop = [&]() -> int {
-        --sp;
-        if (cached) { cached = false; return ctop; }
-        return (SK > 0 && sp < SK) ? sstack[sp][threadIdx.x] : stack[sp - SK];
-    };
-#else
     auto spush = [&](int v) {
         if (SK > 0 && sp < SK) sstack[sp][threadIdx.x] = v;
         else stack[sp - SK] = v;
@@ -295,7 +266,6 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
         --sp;
         return (SK > 0 && sp < SK) ? sstack[sp][threadIdx.x] : stack[sp - SK];
     };
-#endif
     int node = PYRE_NODE_NONE;
     int inst = -1;
     f3 o = r.o;
@@ -328,7 +298,6 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                     hit_any = false;
                     exhausted = root < 0;
                     sp = 0;
-                    PYRE_DROP_TOP;
                     node = exhausted ? PYRE_NODE_NONE : (root | PYRE_TAG_TOP);
                     inst = -1;
                     o = r.o;
@@ -379,7 +348,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                     }
                     float e;
                     if (!slab(I.lo[0], I.hi[0], I.lo[1], I.hi[1], I.lo[2], I.hi[2], lo, inv, r.tmin, best_t, &e)) continue;
-                    if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; PYRE_DROP_TOP; continue; }
+                    if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                     spush(PYRE_NODE_EXIT);
                     inst = k;
                     o = lo;
@@ -426,7 +395,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                     int nh = 0;
     #pragma unroll
                     for (int k = 1; k < WIDTH; ++k) nh += ent[k] != PYRE_NODE_NONE ? 1 : 0;
-                    if (sp + nh > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; PYRE_DROP_TOP; continue; }
+                    if (sp + nh > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
     #pragma unroll
                     for (int k = WIDTH - 1; k >= 1; --k)
                         if (ent[k] != PYRE_NODE_NONE) spush(ent[k]);
@@ -444,7 +413,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                 // leaves: park triangle ranges, or queue the instances of a top-level leaf
                 if (top) {
                     const int need = (h0 && leaf0 ? nd.z : 0) + (h1 && leaf1 ? nd.w : 0) + 1;
-                    if (sp + need > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; PYRE_DROP_TOP; continue; }
+                    if (sp + need > STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                     if (h1 && leaf1)
                         for (int k = nd.w - 1; k >= 0; --k) spush(PYRE_TAG_INST | (nd.y + k));
                     if (h0 && leaf0)
@@ -457,7 +426,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                 const bool g0 = h0 && !leaf0, g1 = h1 && !leaf1;
                 if (g0 && g1) {
                     const bool first0 = e0 <= e1;
-                    if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; PYRE_DROP_TOP; continue; }
+                    if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                     spush((first0 ? nd.y : nd.x) | tag);
                     node = (first0 ? nd.x : nd.y) | tag;
                 } else if (g0) {
