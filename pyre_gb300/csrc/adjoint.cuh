@@ -174,10 +174,6 @@ namespace pyre {
 
 #define PYRE_NO_KEY 0xffffffffu
 #define PYRE_FLUSH_ROUNDS 3  // keys aggregated per flush; the rest add directly
-#ifndef PYRE_FLUSH_UNROLL
-#define PYRE_FLUSH_UNROLL 6  // unroll of the per-parameter / per-texel butterfly loops of a flush
-#endif
-constexpr int kFlushUnroll = PYRE_FLUSH_UNROLL;
 
 // One lane's gradient terms of one path vertex, added at a point where the
 // warp is converged (warp_flush): the 6 parameters of one material (all the
@@ -217,7 +213,7 @@ __device__ __forceinline__ void warp_flush(const DevScene& S, float* env_grad, d
             const uint32_t key = __shfl_sync(FULL, t.mat, src);
             const bool mine = left && t.mat == key;
             todo &= ~__ballot_sync(FULL, mine);
-#pragma unroll (kFlushUnroll)
+#pragma unroll
             for (int k = 0; k < PYRE_NPARAM; ++k) {
                 const double v = warp_sum(mine ? (double)t.g[k] : 0.0);
                 if (lane == src) mat_add(key, k, v);
@@ -247,7 +243,7 @@ __device__ __forceinline__ void warp_flush(const DevScene& S, float* env_grad, d
             const uint32_t k0 = __shfl_sync(FULL, key, src);
             const bool mine = left && key == k0;
             todo &= ~__ballot_sync(FULL, mine);
-#pragma unroll (kFlushUnroll)
+#pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const float x = warp_sum(mine ? c.x * wt[q] : 0.0f), y = warp_sum(mine ? c.y * wt[q] : 0.0f),
                             z = warp_sum(mine ? c.z * wt[q] : 0.0f);

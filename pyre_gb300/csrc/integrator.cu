@@ -468,10 +468,7 @@ __global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
 // registers) by 0.3 % on the 1080p studio frame. The adjoint variant keeps
 // 3 blocks of 256: at 72 registers its spills would grow.
 template <bool BATCH, bool ADJ = false>
-#ifndef PYRE_ADJ_SHADE_BLOCKS
-#define PYRE_ADJ_SHADE_BLOCKS 3
-#endif
-__global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? PYRE_ADJ_SHADE_BLOCKS : 4) k_shade(DevScene S, PathSoA P, WaveParams W,
+__global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene S, PathSoA P, WaveParams W,
                                                                         uint32_t depth) {
     extern __shared__ double sgrad[];
     if (ADJ && W.smem_grad) {
