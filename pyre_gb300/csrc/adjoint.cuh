@@ -147,8 +147,101 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+#define PYRE_NO_KEY 0xffffffffu
+
+// Texel gradients of one block go through a cache in shared memory: a
+// direct-mapped table of PYRE_ENV_CACHE slots, each claimed for good by the
+// first texel that hashes to it and summed with shared-memory atomics; the
+// block adds the table to the gradient once, when it ends. Importance
+// sampling sends most environment terms to the few texels of a bright lobe,
+// and one global atomic per term (even after warp aggregation) queued on
+// those addresses. A texel whose slot another texel holds adds directly.
+#ifndef PYRE_ENV_CACHE_LOG2
+#define PYRE_ENV_CACHE_LOG2 10  // 1024 slots, 20 KB of shared memory per block
+#endif
+#define PYRE_ENV_CACHE (1u << PYRE_ENV_CACHE_LOG2)
+
+// A block's gradient accumulators in its dynamic shared memory: the texel
+// cache (null without texel gradients), then the material sums (null when
+// they add to global memory directly).
+struct GradSmem {
+    float4* cval;    // PYRE_ENV_CACHE texel sums (x, y, z)
+    uint32_t* ckey;  // the texel of each slot, PYRE_NO_KEY while free
+    double* mat;     // n_mat * PYRE_NPARAM material sums
+};
+
+// Bytes of dynamic shared memory for the accumulators.
+__host__ __device__ __forceinline__ size_t grad_smem_bytes(bool env_cache, size_t mat_bytes) {
+    return (env_cache ? (size_t)PYRE_ENV_CACHE * (sizeof(float4) + sizeof(uint32_t)) : 0) + mat_bytes;
+}
+
+// Lays out and clears the block's accumulators (all threads of the block call it).
+__device__ __forceinline__ GradSmem grad_smem_begin(bool env_cache, bool mat_smem, uint32_t n_mat) {
+    extern __shared__ float4 grad_dyn_smem[];
+    GradSmem G;
+    char* p = reinterpret_cast<char*>(grad_dyn_smem);
+    G.cval = nullptr; G.ckey = nullptr; G.mat = nullptr;
+    if (env_cache) {
+        G.cval = reinterpret_cast<float4*>(p);
+        G.ckey = reinterpret_cast<uint32_t*>(p + PYRE_ENV_CACHE * sizeof(float4));
+        p += PYRE_ENV_CACHE * (sizeof(float4) + sizeof(uint32_t));
+        for (uint32_t k = threadIdx.x; k < PYRE_ENV_CACHE; k += blockDim.x) {
+            G.cval[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            G.ckey[k] = PYRE_NO_KEY;
+        }
+    }
+    if (mat_smem) {
+        G.mat = reinterpret_cast<double*>(p);
+        for (uint32_t k = threadIdx.x; k < n_mat * PYRE_NPARAM; k += blockDim.x) G.mat[k] = 0.0;
+    }
+    __syncthreads();
+    return G;
+}
+
+// Adds the block's accumulators to the gradients (all threads of the block call it).
+__device__ __forceinline__ void grad_smem_end(const GradSmem& G, float* env_grad, double* mat_grad, uint32_t n_mat) {
+    if (!G.cval && !G.mat) return;
+    __syncthreads();
+    if (G.cval)
+        for (uint32_t k = threadIdx.x; k < PYRE_ENV_CACHE; k += blockDim.x) {
+            const uint32_t t = G.ckey[k];
+            if (t == PYRE_NO_KEY) continue;
+            const float4 v = G.cval[k];
+            if (v.x != 0.0f) atomicAdd(env_grad + 3 * (size_t)t, v.x);
+            if (v.y != 0.0f) atomicAdd(env_grad + 3 * (size_t)t + 1, v.y);
+            if (v.z != 0.0f) atomicAdd(env_grad + 3 * (size_t)t + 2, v.z);
+        }
+    if (G.mat)
+        for (uint32_t k = threadIdx.x; k < n_mat * PYRE_NPARAM; k += blockDim.x)
+            if (G.mat[k] != 0.0) atomicAdd(mat_grad + k, G.mat[k]);
+}
+
+// d(loss)/d(texel t) += (x, y, z), through the block's cache when it has one.
+__device__ __forceinline__ void env_grad_add(float* env_grad, const GradSmem& G, uint32_t t, float x, float y,
+                                             float z) {
+    if (G.ckey) {
+        const uint32_t slot = (t * 2654435761u) >> (32 - PYRE_ENV_CACHE_LOG2);
+        uint32_t k = *reinterpret_cast<volatile uint32_t*>(G.ckey + slot);
+        if (k == PYRE_NO_KEY) {
+            const uint32_t old = atomicCAS(G.ckey + slot, PYRE_NO_KEY, t);
+            k = old == PYRE_NO_KEY ? t : old;
+        }
+        if (k == t) {
+            float* v = reinterpret_cast<float*>(G.cval + slot);
+            if (x != 0.0f) atomicAdd(v, x);
+            if (y != 0.0f) atomicAdd(v + 1, y);
+            if (z != 0.0f) atomicAdd(v + 2, z);
+            return;
+        }
+    }
+    const size_t a = 3 * (size_t)t;
+    if (x != 0.0f) atomicAdd(env_grad + a, x);
+    if (y != 0.0f) atomicAdd(env_grad + a + 1, y);
+    if (z != 0.0f) atomicAdd(env_grad + a + 2, z);
+}
+
 // d(loss)/d(texel) for a radiance term c * Le(uv), Le = texture(uv) * intensity.
-__device__ __forceinline__ void scatter_env(const DevEnv& E, float* env_grad, f2 uv, f3 c) {
+__device__ __forceinline__ void scatter_env(const DevEnv& E, float* env_grad, const GradSmem& G, f2 uv, f3 c) {
     if (!env_grad) return;
     uint32_t idx[4];
     float wt[4];
@@ -162,9 +255,7 @@ __device__ __forceinline__ void scatter_env(const DevEnv& E, float* env_grad, f2
         const unsigned peers = __match_any_sync(act, key);
         const float x = peer_sum(peers, c.x * s), y = peer_sum(peers, c.y * s), z = peer_sum(peers, c.z * s);
         if (key == 0xffffffffu || lane != __ffs(peers) - 1) continue;
-        atomicAdd(env_grad + 3 * (size_t)key, x);
-        atomicAdd(env_grad + 3 * (size_t)key + 1, y);
-        atomicAdd(env_grad + 3 * (size_t)key + 2, z);
+        env_grad_add(env_grad, G, key, x, y, z);
     }
 }
 
@@ -172,7 +263,6 @@ __device__ __forceinline__ void scatter_env(const DevEnv& E, float* env_grad, f2
 
 namespace pyre {
 
-#define PYRE_NO_KEY 0xffffffffu
 #define PYRE_FLUSH_ROUNDS 3  // keys aggregated per flush; the rest add directly
 
 // One lane's gradient terms of one path vertex, added at a point where the
@@ -192,14 +282,14 @@ struct GradTerms {
 // (FP64 for materials), for up to PYRE_FLUSH_ROUNDS keys per kind that more
 // than one lane holds, and one lane adds each sum; every other lane adds its
 // own terms. A warp that is not converged adds lane by lane.
-__device__ __forceinline__ void warp_flush(const DevScene& S, float* env_grad, double* mat_grad, double* sgrad,
-                                           bool smem, const GradTerms& t) {
+__device__ __forceinline__ void warp_flush(const DevScene& S, float* env_grad, double* mat_grad, const GradSmem& G,
+                                           const GradTerms& t) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const bool full = __activemask() == FULL;
     auto mat_add = [&](uint32_t m, int k, double v) {
         if (v == 0.0) return;
-        if (smem) atomicAdd(sgrad + PYRE_NPARAM * m + k, v);
+        if (G.mat) atomicAdd(G.mat + PYRE_NPARAM * m + k, v);
         else atomicAdd(mat_grad + PYRE_NPARAM * (size_t)m + k, v);
     };
     // materials
@@ -247,12 +337,7 @@ __device__ __forceinline__ void warp_flush(const DevScene& S, float* env_grad, d
             for (int q = 0; q < 4; ++q) {
                 const float x = warp_sum(mine ? c.x * wt[q] : 0.0f), y = warp_sum(mine ? c.y * wt[q] : 0.0f),
                             z = warp_sum(mine ? c.z * wt[q] : 0.0f);
-                if (lane == src) {
-                    const size_t a = 3 * (size_t)idx[q];
-                    if (x != 0.0f) atomicAdd(env_grad + a, x);
-                    if (y != 0.0f) atomicAdd(env_grad + a + 1, y);
-                    if (z != 0.0f) atomicAdd(env_grad + a + 2, z);
-                }
+                if (lane == src) env_grad_add(env_grad, G, idx[q], x, y, z);
             }
             if (mine) left = false;
         }
@@ -260,10 +345,7 @@ __device__ __forceinline__ void warp_flush(const DevScene& S, float* env_grad, d
     if (left)
         for (int q = 0; q < 4; ++q) {
             if (wt[q] == 0.0f) continue;
-            const size_t a = 3 * (size_t)idx[q];
-            atomicAdd(env_grad + a, c.x * wt[q]);
-            atomicAdd(env_grad + a + 1, c.y * wt[q]);
-            atomicAdd(env_grad + a + 2, c.z * wt[q]);
+            env_grad_add(env_grad, G, idx[q], c.x * wt[q], c.y * wt[q], c.z * wt[q]);
         }
 }
 

@@ -32,6 +32,13 @@ namespace cg = cooperative_groups;
 namespace pyre {
 
 #define PYRE_MAX_DEPTH 64
+// resident blocks of 128 threads per SM for closest-hit (extend, ray queries) and any-hit (shadow) traversal
+#ifndef PYRE_TRACE_BLOCKS
+#define PYRE_TRACE_BLOCKS 9
+#endif
+#ifndef PYRE_TRACE_BLOCKS_ANY
+#define PYRE_TRACE_BLOCKS_ANY 9
+#endif
 #define PYRE_SORT_BINS 1024  // shade-queue sort keys: escaped, light hit, then materials
 
 struct WaveCtl {
@@ -88,6 +95,7 @@ struct WaveParams {
     float* env_grad;     // env texels*3 or null
     uint32_t n_mat;
     int smem_grad;       // material gradients summed per block in shared memory
+    int env_cache;       // texel gradients summed per block through a shared-memory cache
     int refill;          // traversal: idle lanes of a warp that trigger a refetch (closest hit)
     int refill_any;      // the same for the any-hit (shadow) traversal
     int sort;            // shade reads the live paths sorted by material (P.qsort)
@@ -330,7 +338,7 @@ struct ExtendRays {
 // frame 9 blocks beat 8 (64 registers) by 2 %, and 8 beat the 7 of the
 // unconstrained 70-register build by 2 %; 10 blocks (48 registers) lose 2 %.
 template <bool BATCH, int WIDTH>
-__global__ void __launch_bounds__(128, 9) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+__global__ void __launch_bounds__(128, PYRE_TRACE_BLOCKS) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1], depth};
     trace_stream<false, WIDTH>(S, src, P.ctl->count[depth], &P.ctl->fetch[2 * depth], W.refill);
 }
@@ -363,7 +371,7 @@ struct ShadowRays {
 };
 
 template <bool BATCH, int WIDTH>
-__global__ void __launch_bounds__(128, 9) k_shadow(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
+__global__ void __launch_bounds__(128, PYRE_TRACE_BLOCKS_ANY) k_shadow(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ShadowRays<BATCH> src{&S, &P, &W};
     trace_stream<true, WIDTH>(S, src, P.ctl->scount[depth], &P.ctl->fetch[2 * depth + 1], W.refill_any);
 }
@@ -470,11 +478,8 @@ __global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
 template <bool BATCH, bool ADJ = false>
 __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene S, PathSoA P, WaveParams W,
                                                                         uint32_t depth) {
-    extern __shared__ double sgrad[];
-    if (ADJ && W.smem_grad) {
-        for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x) sgrad[k] = 0.0;
-        __syncthreads();
-    }
+    GradSmem G{nullptr, nullptr, nullptr};
+    if (ADJ) G = grad_smem_begin(W.env_cache != 0, W.smem_grad != 0, W.n_mat);
     const uint32_t n = P.ctl->count[depth];
     const uint32_t* qin = P.q[depth & 1];
     uint32_t* qout = P.q[(depth + 1) & 1];
@@ -528,7 +533,7 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
                 }
             }
         }
-        if (ADJ) warp_flush(S, W.env_grad, W.mat_grad, sgrad, W.smem_grad != 0, gt);
+        if (ADJ) warp_flush(S, W.env_grad, W.mat_grad, G, gt);
         const float4 bq = depth > 0 ? __ldcs(P.beta + i) : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         f3 beta = mk3(bq.x, bq.y, bq.z);
         const float last_pdf = bq.w;
@@ -557,7 +562,7 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
                         w_adj = w;
                     }
                     // d/d texels of beta * texture(uv) * intensity * w
-                    if (ADJ) scatter_env(S.env, W.env_grad, uv, delta * beta * w_adj);
+                    if (ADJ) scatter_env(S.env, W.env_grad, G, uv, delta * beta * w_adj);
                 }
             }
         } else if (code <= -2) {
@@ -717,33 +722,21 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
         }
         __stcs(P.L + i, make_float4(L.x, L.y, L.z, 0.0f));
     }
-    if (ADJ && W.smem_grad) {  // one FP64 atomic per parameter per block
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x)
-            if (sgrad[k] != 0.0) atomicAdd(W.mat_grad + k, sgrad[k]);
-    }
+    if (ADJ) grad_smem_end(G, W.env_grad, W.mat_grad, W.n_mat);  // one atomic per parameter / texel per block
 }
 
 // Adjoint replay: parked gradient terms of the paths' last vertices.
 __global__ void k_accumulate_adjoint(DevScene S, PathSoA P, WaveParams W) {
-    extern __shared__ double sgrad[];
-    if (W.smem_grad) {
-        for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x) sgrad[k] = 0.0;
-        __syncthreads();
-    }
+    const GradSmem G = grad_smem_begin(W.env_cache != 0, W.smem_grad != 0, W.n_mat);
     const uint32_t n = P.ctl->n_valid;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         GradTerms gt;
         for (uint32_t s = 0; s < W.ns; ++s)
             if (P.pend[(size_t)i * W.ns + s].w != 0.0f)
                 collect_parked_grad(P.gpend + PYRE_GSLOT * ((size_t)i * W.ns + s), gt);
-        warp_flush(S, W.env_grad, W.mat_grad, sgrad, W.smem_grad != 0, gt);
+        warp_flush(S, W.env_grad, W.mat_grad, G, gt);
     }
-    if (W.smem_grad) {
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < W.n_mat * PYRE_NPARAM; k += blockDim.x)
-            if (sgrad[k] != 0.0) atomicAdd(W.mat_grad + k, sgrad[k]);
-    }
+    grad_smem_end(G, W.env_grad, W.mat_grad, W.n_mat);
 }
 
 // ------------------------------------------------------------ accumulate --
@@ -881,7 +874,7 @@ struct QueryRays {
 };
 
 template <bool ANY, int WIDTH>
-__global__ void __launch_bounds__(128, 9) k_intersect(DevScene S, QueryRays q, uint32_t n, unsigned int* counter,
+__global__ void __launch_bounds__(128, PYRE_TRACE_BLOCKS) k_intersect(DevScene S, QueryRays q, uint32_t n, unsigned int* counter,
                                                    int refill) {
     QueryRays src = q;
     src.S = &S;
@@ -1852,8 +1845,10 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     W.mat_grad = d_mat;
     W.env_grad = (env_elems && grads->env) ? d_env : nullptr;
     W.n_mat = n_mat;
-    const size_t smem = mat_bytes <= 48 * 1024 ? mat_bytes : 0;
-    W.smem_grad = smem ? 1 : 0;
+    W.env_cache = W.env_grad ? 1 : 0;
+    const size_t mat_smem = grad_smem_bytes(W.env_cache, mat_bytes) <= 48 * 1024 ? mat_bytes : 0;
+    W.smem_grad = mat_smem ? 1 : 0;
+    const size_t smem = grad_smem_bytes(W.env_cache, mat_smem);
 
     const Launch Lc = make_launch<false>(ctx, rp.block_size, W.bvh_width);
     const int grid_adj = grid_for(ctx, k_shade<false, true>, Lc.block_stage, smem);
