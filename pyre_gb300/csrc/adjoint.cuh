@@ -160,6 +160,9 @@ __device__ __forceinline__ T warp_sum(T v) {
 #define PYRE_ENV_CACHE_LOG2 10  // 1024 slots, 20 KB of shared memory per block
 #endif
 #define PYRE_ENV_CACHE (1u << PYRE_ENV_CACHE_LOG2)
+#ifndef PYRE_ENV_CACHE_DIRECT
+#define PYRE_ENV_CACHE_DIRECT 0  // lanes add texel terms to the cache one by one, without warp aggregation
+#endif
 
 // A block's gradient accumulators in its dynamic shared memory: the texel
 // cache (null without texel gradients), then the material sums (null when
@@ -246,6 +249,15 @@ __device__ __forceinline__ void scatter_env(const DevEnv& E, float* env_grad, co
     uint32_t idx[4];
     float wt[4];
     env_texel_weights(E, uv, idx, wt);
+#if PYRE_ENV_CACHE_DIRECT
+    if (G.ckey) {
+        for (int k = 0; k < 4; ++k) {
+            const float s = wt[k] * E.intensity;
+            if (s != 0.0f) env_grad_add(env_grad, G, idx[k], c.x * s, c.y * s, c.z * s);
+        }
+        return;
+    }
+#endif
     const unsigned act = __activemask();
     const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -286,7 +298,7 @@ __device__ __forceinline__ void warp_flush(const DevScene& S, float* env_grad, d
                                            const GradTerms& t) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const bool full = __activemask() == FULL;
+    bool full = __activemask() == FULL;
     auto mat_add = [&](uint32_t m, int k, double v) {
         if (v == 0.0) return;
         if (G.mat) atomicAdd(G.mat + PYRE_NPARAM * m + k, v);
@@ -325,6 +337,11 @@ __device__ __forceinline__ void warp_flush(const DevScene& S, float* env_grad, d
         c = t.c * S.env.intensity;
     }
     left = key != PYRE_NO_KEY;
+#if PYRE_ENV_CACHE_DIRECT
+    // with the block's cache the lanes add their own terms: shared-memory
+    // atomics on one slot cost less than the warp's butterflies
+    if (G.ckey) full = false;
+#endif
     if (full) {
         const unsigned peers = __match_any_sync(FULL, key);
         unsigned todo = __ballot_sync(FULL, left && (peers & (peers - 1u)) != 0u);
