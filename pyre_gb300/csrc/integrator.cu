@@ -33,8 +33,10 @@ namespace pyre {
 
 #define PYRE_MAX_DEPTH 64
 // resident blocks of 128 threads per SM for closest-hit (extend, ray queries) and any-hit (shadow) traversal
+// (closest hit: 10 blocks at 48 registers measured 705.9 against 703.5
+// Msamples/s for 9; any hit keeps 9: 10 took 38.5 against 36.5 ms of shadow)
 #ifndef PYRE_TRACE_BLOCKS
-#define PYRE_TRACE_BLOCKS 9
+#define PYRE_TRACE_BLOCKS 10
 #endif
 #ifndef PYRE_TRACE_BLOCKS_ANY
 #define PYRE_TRACE_BLOCKS_ANY 9
@@ -332,11 +334,11 @@ struct ExtendRays {
     }
 };
 
-// The traversal kernels ask for 9 resident blocks of 128 threads (at most 56
-// registers; k_extend spills a few dozen bytes). Warps wait mostly on node,
-// triangle and stack loads, so more of them per SM pay. On the 1080p studio
-// frame 9 blocks beat 8 (64 registers) by 2 %, and 8 beat the 7 of the
-// unconstrained 70-register build by 2 %; 10 blocks (48 registers) lose 2 %.
+// The traversal kernels are persistent grids of resident 128-thread blocks:
+// 10 per SM for closest hit (48 registers, about 100 bytes of spills) and 9
+// for any hit (56 registers, no spills). Warps wait mostly on node, triangle
+// and stack loads, so more of them per SM pay, up to where the spills cost
+// more than the extra warps hide.
 template <bool BATCH, int WIDTH>
 __global__ void __launch_bounds__(128, PYRE_TRACE_BLOCKS) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1], depth};
@@ -874,7 +876,7 @@ struct QueryRays {
 };
 
 template <bool ANY, int WIDTH>
-__global__ void __launch_bounds__(128, PYRE_TRACE_BLOCKS) k_intersect(DevScene S, QueryRays q, uint32_t n, unsigned int* counter,
+__global__ void __launch_bounds__(128, ANY ? PYRE_TRACE_BLOCKS_ANY : PYRE_TRACE_BLOCKS) k_intersect(DevScene S, QueryRays q, uint32_t n, unsigned int* counter,
                                                    int refill) {
     QueryRays src = q;
     src.S = &S;
