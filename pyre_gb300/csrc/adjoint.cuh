@@ -167,8 +167,10 @@ __device__ __forceinline__ T warp_sum(T v) {
 #ifndef PYRE_ENV_CACHE_DIRECT
 #define PYRE_ENV_CACHE_DIRECT 1
 #endif
+// The same for the material terms when the block sums them in shared memory
+// (FP64): 23.9 against 24.6 ms.
 #ifndef PYRE_MAT_DIRECT
-#define PYRE_MAT_DIRECT 0  // lanes add material terms to the block's FP64 sums directly
+#define PYRE_MAT_DIRECT 1
 #endif
 
 // A block's gradient accumulators in its dynamic shared memory: the texel
