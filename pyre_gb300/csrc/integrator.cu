@@ -1847,10 +1847,7 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     W.mat_grad = d_mat;
     W.env_grad = (env_elems && grads->env) ? d_env : nullptr;
     W.n_mat = n_mat;
-#ifndef PYRE_ENV_CACHE_ENABLE
-#define PYRE_ENV_CACHE_ENABLE 1
-#endif
-    W.env_cache = (PYRE_ENV_CACHE_ENABLE && W.env_grad) ? 1 : 0;
+    W.env_cache = W.env_grad ? 1 : 0;
     const size_t mat_smem = grad_smem_bytes(W.env_cache, mat_bytes) <= 48 * 1024 ? mat_bytes : 0;
     W.smem_grad = mat_smem ? 1 : 0;
     const size_t smem = grad_smem_bytes(W.env_cache, mat_smem);
