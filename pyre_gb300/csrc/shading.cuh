@@ -8,18 +8,6 @@
 #include "../../include/pyre_cuda.h"
 #include "device_scene.cuh"
 
-// Code that the headline frame never runs (quad-light sampling and pdf, the
-// CDF mode of environment sampling) can be kept out of line, so the shade
-// kernel's hot path spans fewer instruction-cache lines.
-#ifndef PYRE_COLD_OUT_OF_LINE
-#define PYRE_COLD_OUT_OF_LINE 0
-#endif
-#if PYRE_COLD_OUT_OF_LINE
-#define PYRE_COLD static __device__ __noinline__
-#else
-#define PYRE_COLD __device__ __forceinline__
-#endif
-
 namespace pyre {
 
 // ---------------------------------------------------------------- frame ----
@@ -246,7 +234,7 @@ __device__ __forceinline__ bool bsdf_sample(const Bsdf& b, f3 wo, f2 u, f3* wi_o
 
 // ---------------------------------------------------------- quad lights ----
 // DiffuseAreaQuadLight::sample, light.rs:111-133
-PYRE_COLD bool quad_sample(const DevQuadLight& L, f3 from, f2 u, f3* pos, f3* wi_out, float* pdf) {
+__device__ __forceinline__ bool quad_sample(const DevQuadLight& L, f3 from, f2 u, f3* pos, f3* wi_out, float* pdf) {
     f3 p = L.p0 + u.x * L.edge_u + u.y * L.edge_v;
     f3 to_light = p - from;
     float dist2 = len2(to_light);
@@ -261,7 +249,7 @@ PYRE_COLD bool quad_sample(const DevQuadLight& L, f3 from, f2 u, f3* pos, f3* wi
     return true;
 }
 // DiffuseAreaQuadLight::pdf, light.rs:135-144
-PYRE_COLD float quad_pdf(const DevQuadLight& L, f3 from, f3 wi) {
+__device__ __forceinline__ float quad_pdf(const DevQuadLight& L, f3 from, f3 wi) {
     float t; f3 p;
     if (!quad_intersect(L, from, wi, 1e-4f, __int_as_float(0x7f800000), &t, &p)) return 0.0f;
     float cos_light = -dot3(wi, L.normal);
@@ -336,7 +324,7 @@ __device__ __forceinline__ float env_pdf_at(const DevEnv& E, f2 uv) {
 }
 
 // Distribution1D::sample_continuous (distribution.rs:79-101) over a CDF row.
-PYRE_COLD float cdf_sample(const float* cdf, uint32_t n, float u, float* pdf, uint32_t* bin_out) {
+__device__ __forceinline__ float cdf_sample(const float* cdf, uint32_t n, float u, float* pdf, uint32_t* bin_out) {
     uint32_t lo = 1, hi = n;
     while (lo < hi) {
         uint32_t mid = (lo + hi) / 2;
