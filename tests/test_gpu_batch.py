@@ -62,3 +62,48 @@ def test_batch_rejects_bad_part(gpu_ctx):
     with pytest.raises(PyreError):
         gpu_ctx.render_batch(ds, spec)
     ds.close()
+
+
+@pytest.mark.parametrize("use_graph", [0, 1])
+def test_batch_device_films_and_missing_channels(gpu_ctx, use_graph):
+    """Films in device memory (copied on the library's second stream while later waves render) and films with
+    some channels left NULL get the same bits as host films, over several waves."""
+    import ctypes as C
+
+    import torch
+
+    from pyre_gb300 import native as N
+    jobs = _jobs()
+    ds = gpu_ctx.upload_batch([j["scene"] for j in jobs])
+    spec = [{"part": k, "camera": j["camera"], "width": j["width"], "height": j["height"], "spp": j["spp"],
+             "integrator": j["integrator"]} for k, j in enumerate(jobs)]
+    ref = gpu_ctx.render_batch(ds, spec, wave_paths=9000)
+    dev, cjobs = [], []
+    for k, j in enumerate(jobs):
+        npix = j["width"] * j["height"]
+        t = {c: torch.full((npix * n,), -1.0, dtype=torch.float32, device="cuda")
+             for c, n in (("radiance", 3), ("albedo", 3), ("normal", 3), ("depth", 1))}
+        dev.append(t)
+        b = N.BatchJob()
+        b.part, b.camera = k, j["camera"].to_desc()
+        b.width, b.height, b.spp_begin, b.spp_end = j["width"], j["height"], 0, j["spp"]
+        b.max_depth, b.min_rr_depth = j["integrator"].max_depth, j["integrator"].min_rr_depth
+        # odd jobs leave albedo and normal out
+        skip = k % 2 == 1
+        b.film = N.Film(N.dptr(t["radiance"]), None if skip else N.dptr(t["albedo"]),
+                        None if skip else N.dptr(t["normal"]), N.dptr(t["depth"]), N.PYRE_MEM_DEVICE)
+        cjobs.append(b)
+    arr = (N.BatchJob * len(cjobs))(*cjobs)
+    p = N.RenderParams()
+    p.wave_paths, p.use_graph = 9000, use_graph
+    gpu_ctx.check(gpu_ctx.lib.pyre_render_batch(gpu_ctx.handle, ds.handle, arr, len(cjobs), C.byref(p)))
+    assert gpu_ctx.stats().waves > 1
+    for k, (t, f) in enumerate(zip(dev, ref)):
+        np.testing.assert_array_equal(t["radiance"].cpu().numpy().reshape(f.radiance.shape), f.radiance)
+        np.testing.assert_array_equal(t["depth"].cpu().numpy().reshape(f.depth.shape), f.depth)
+        if k % 2 == 1:
+            assert bool((t["albedo"] == -1.0).all()) and bool((t["normal"] == -1.0).all())
+        else:
+            np.testing.assert_array_equal(t["albedo"].cpu().numpy().reshape(f.albedo.shape), f.albedo)
+            np.testing.assert_array_equal(t["normal"].cpu().numpy().reshape(f.normal.shape), f.normal)
+    ds.close()
