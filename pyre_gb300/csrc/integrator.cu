@@ -109,8 +109,12 @@ struct WaveParams {
 
 // Default ray-refill thresholds (idle lanes of a warp) of closest-hit and
 // any-hit traversal; a nonzero refill_lanes sets both.
+#ifndef PYRE_DEFAULT_REFILL
 #define PYRE_DEFAULT_REFILL 16
+#endif
+#ifndef PYRE_DEFAULT_REFILL_ANY
 #define PYRE_DEFAULT_REFILL_ANY 8
+#endif
 static inline int refill_lanes(const pyre_render_params* rp, bool any_hit = false) {
     const uint32_t v = rp ? rp->refill_lanes : 0u;
     if (v == 0) return any_hit ? PYRE_DEFAULT_REFILL_ANY : PYRE_DEFAULT_REFILL;
