@@ -75,6 +75,53 @@ def test_cornell_scenes(gpu_ctx, oracle_mod, name, width):
                           osc.occluded(org, d, np.full_like(tm, 1e-3), tm))
 
 
+def _axis_rays():
+    """Origins on a grid whose values include the Cornell box's node planes (the walls at +-1), and directions
+    with zero components of either sign, so that 1/d is +inf or -inf and (plane - origin) * (1/d) is 0 * inf."""
+    vals = np.array([-1.0, -0.999, -0.5, -0.125, -0.0, 0.0, 0.125, 0.3, 0.999, 1.0], np.float32)
+    org = np.stack(np.meshgrid(vals, vals, vals, indexing="ij"), -1).reshape(-1, 3)
+    dirs = []
+    for a in range(3):
+        b, c = (a + 1) % 3, (a + 2) % 3
+        for s in (1.0, -1.0):
+            for zb in (0.0, -0.0):
+                for zc in (0.0, -0.0):
+                    d = [0.0] * 3
+                    d[a], d[b], d[c] = s, zb, zc
+                    dirs.append(d)
+        for sa in (0.6, -0.6):
+            for sb in (0.8, -0.8):
+                for zc in (0.0, -0.0):
+                    d = [0.0] * 3
+                    d[a], d[b], d[c] = sa, sb, zc
+                    dirs.append(d)
+    dirs = np.array(dirs, np.float32)
+    o = np.repeat(org, len(dirs), axis=0)
+    d = np.tile(dirs, (len(org), 1))
+    return np.ascontiguousarray(o), np.ascontiguousarray(d)
+
+
+@pytest.mark.parametrize("width", [2, 4, 8])
+def test_axis_aligned_rays_on_node_planes(gpu_ctx, oracle_mod, width):
+    """Rays that make the slab test (bvh.rs:146-153) multiply 0 by an infinity: its min / max reductions then
+    see NaN operands, which Rust's f32::min / f32::max (and the kernels' min / max) ignore. Hits, t/u/v and
+    occlusion answers must be the oracle's, closest hit and any hit."""
+    sc = P.cornell_box()
+    org, d = _axis_rays()
+    assert np.signbit(d).any() and (d == 0).any()
+    n = org.shape[0]
+    tmin, tmax = np.full(n, 1e-4, np.float32), np.full(n, np.inf, np.float32)
+    ds = gpu_ctx.upload(sc)
+    ds.set_bvh_width(width)
+    osc = oracle_mod.OracleScene(sc)
+    r = osc.intersect(org, d, tmin, tmax)
+    assert (r["kind"] > 0).mean() > 0.5
+    _compare(gpu_ctx.intersect(ds, org, d, tmin, tmax), r, "axis-aligned")
+    for t_hi in (0.5, 1.0, np.inf):
+        tm = np.full(n, t_hi, np.float32)
+        assert np.array_equal(gpu_ctx.intersect(ds, org, d, tmin, tm, any_hit=True), osc.occluded(org, d, tmin, tm))
+
+
 @pytest.mark.parametrize("width", [2, 4, 8])
 def test_motion_blur_instances(gpu_ctx, oracle_mod, width):
     sc = Scene()
