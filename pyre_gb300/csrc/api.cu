@@ -512,10 +512,24 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
         if (live.empty()) continue;
         std::vector<pyre_bvh2_node> tn;
         std::vector<uint32_t> tp;
-        build_bvh2(ibox, icent, tn, tp);
+        build_bvh2(ibox, icent, tn, tp, PYRE_TLAS_ENTER ? 1u : 8u);
         const int32_t slot_base = (int32_t)inst.size();
         part_tlas[part] = node_off + (int32_t)nodes.size();
+        const size_t first_top = nodes.size();
         collapse_bvh2(tn.data(), (uint32_t)tn.size(), node_off + (int32_t)nodes.size(), slot_base, nodes);
+        // A top-level leaf of one static instance holds that instance's root
+        // box, unpadded, and the child entry INST|TOP|slot with count -1: the
+        // top-level step's test of the box is the reference's root test
+        // (bvh.rs:103-110) and the lane then enters the instance without a
+        // node step of its own.
+        for (size_t g = first_top; PYRE_TLAS_ENTER && g < nodes.size(); ++g)
+            for (int c = 0; c < 2; ++c) {
+                if (nodes[g].d[2 + c] != 1) continue;
+                const int32_t slot = nodes[g].d[c];
+                const pyre_instance_desc& id = desc->instances[live[tp[(size_t)(slot - slot_base)]]];
+                if (id.has_motion) continue;
+                set_gpu_child(nodes[g], c, mesh_box[id.mesh], slot | PYRE_TAG_INST | PYRE_TAG_TOP, -1);
+            }
         inst.resize(inst.size() + tp.size());
         for (size_t k = 0; k < tp.size(); ++k) {
             uint32_t i = live[tp[k]];

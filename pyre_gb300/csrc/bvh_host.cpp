@@ -20,7 +20,6 @@ namespace pyre {
 namespace {
 
 const int kBins = 12;
-const uint32_t kMaxLeaf = 8;
 const float kInf = std::numeric_limits<float>::infinity();
 
 inline Aabb empty_box() { Aabb b; b.lo = splat3(kInf); b.hi = splat3(-kInf); return b; }
@@ -67,7 +66,7 @@ void triangle_bounds(const float* positions, const uint32_t* indices, uint32_t n
 }
 
 void build_bvh2(const std::vector<Aabb>& pb, const std::vector<f3>& pc,
-                std::vector<pyre_bvh2_node>& nodes, std::vector<uint32_t>& idx) {
+                std::vector<pyre_bvh2_node>& nodes, std::vector<uint32_t>& idx, uint32_t max_leaf) {
     const uint32_t n_all = (uint32_t)pb.size();
     idx.resize(n_all);
     for (uint32_t i = 0; i < n_all; ++i) idx[i] = i;
@@ -148,14 +147,14 @@ void build_bvh2(const std::vector<Aabb>& pb, const std::vector<f3>& pc,
         if (!std::isfinite(best)) {
             mid = partition(start, end, axis, cmin + 0.5f * extent);
             if (mid == start || mid == end) {
-                if (n <= kMaxLeaf) { emit(box, start, (uint16_t)n, 0); continue; }
+                if (n <= max_leaf) { emit(box, start, (uint16_t)n, 0); continue; }
                 mid = start + n / 2;
             }
         } else {
-            if (n <= kMaxLeaf && best >= 2.0f * (float)n) { emit(box, start, (uint16_t)n, 0); continue; }
+            if (n <= max_leaf && best >= 2.0f * (float)n) { emit(box, start, (uint16_t)n, 0); continue; }
             mid = partition(start, end, axis, cmin + (float)(best_i + 1) * extent / (float)kBins);
             if (mid == start || mid == end) {
-                if (n <= kMaxLeaf) { emit(box, start, (uint16_t)n, 0); continue; }
+                if (n <= max_leaf) { emit(box, start, (uint16_t)n, 0); continue; }
                 mid = start + n / 2;
             }
         }
@@ -210,6 +209,10 @@ inline void set_child(GpuNode& g, int slot, const Aabb& b, int32_t child, int32_
     g.d[2 + slot] = count;
 }
 }  // namespace
+
+void set_gpu_child(GpuNode& g, int slot, const Aabb& box, int32_t child, int32_t count) {
+    set_child(g, slot, box, child, count);
+}
 
 Aabb collapse_bvh2(const pyre_bvh2_node* nodes, uint32_t n_nodes, int32_t node_base, int32_t slot_base,
                    std::vector<GpuNode>& out) {

@@ -33,8 +33,14 @@ static_assert(sizeof(GpuNode) == 64, "GpuNode is one 64-byte line");
 // Builds the reference's binned-SAH binary BVH (bvh.rs:45-64,180-409) over
 // arbitrary primitive bounds/centroids. Output uses the reference node layout
 // (pyre_bvh2_node): DFS pre-order, left child = index + 1.
+// `max_leaf` bounds the primitives of a leaf (MAX_PRIMS_PER_LEAF = 8,
+// bvh.rs:14); with 1 every primitive gets its own leaf unless centroids
+// coincide.
 void build_bvh2(const std::vector<Aabb>& prim_bounds, const std::vector<f3>& prim_centroids,
-                std::vector<pyre_bvh2_node>& nodes, std::vector<uint32_t>& prim_indices);
+                std::vector<pyre_bvh2_node>& nodes, std::vector<uint32_t>& prim_indices, uint32_t max_leaf = 8);
+
+// Sets child `slot` (0 or 1) of a device node: its box, child and count.
+void set_gpu_child(GpuNode& g, int slot, const Aabb& box, int32_t child, int32_t count);
 
 // Per-triangle bounds and centroids as MeshInstance::build computes them
 // (mesh.rs:77-87, triangle_bounds / triangle_centroid mesh.rs:32-40).

@@ -174,6 +174,8 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 //   [0, 2^29)          node of an instance BVH
 //   TOP | n            node of the top-level BVH
 //   INST | slot        enter instance `slot` (root-box test, local origin)
+//   INST | TOP | slot  enter static instance `slot`, whose root box the
+//                      top-level step already tested
 //   LEAF | n*W + k     leaf child k of wide node n (WIDTH > 2)
 // A lane inside an instance leaves it (restores the world origin) when it
 // reaches the next TOP or INST entry: those lie below the instance's nodes.
@@ -198,6 +200,11 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 #define PYRE_TAG_TOP (1 << 29)
 #define PYRE_TAG_INST (1 << 30)
 #define PYRE_NODE_NONE (-1)
+// top-level leaves of one static instance are entered from the top-level
+// step (INST|TOP entries); 0 keeps every instance behind an INST entry
+#ifndef PYRE_TLAS_ENTER
+#define PYRE_TLAS_ENTER 1
+#endif
 
 // Compare-exchange of (entry distance, stack entry) pairs, ascending.
 __device__ __forceinline__ void cmp_swap(float& ea, int& na, float& eb, int& nb) {
@@ -338,7 +345,15 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                     inst = -1;
                     o = r.o;
                 }
-                if (node & PYRE_TAG_INST) {
+                if ((node & (PYRE_TAG_INST | PYRE_TAG_TOP)) == (PYRE_TAG_INST | PYRE_TAG_TOP)) {
+                    // a static instance whose root box the top-level step
+                    // tested: enter it and step its root node in this step
+                    // (the lane is at the top level, so o is the world origin)
+                    const int k = node & ~(PYRE_TAG_INST | PYRE_TAG_TOP);
+                    node = WIDTH > 2 ? __ldg(S.wroot + k) : __ldg(&S.inst[k].blas_root);
+                    if (node < 0) { node = PYRE_NODE_NONE; continue; }
+                    inst = k;
+                } else if (node & PYRE_TAG_INST) {
                     if (parked) { spush(node); node = PYRE_NODE_NONE; parked = STOP; continue; }
                     const int k = node & ~PYRE_TAG_INST;
                     node = PYRE_NODE_NONE;
