@@ -102,9 +102,11 @@ struct TraceHit {
 // lanes of a warp that may still be looking for a leaf when the leaf phase
 // starts, for closest-hit and any-hit traversal
 // (with two node steps per vote: 12 and 16 against 8 and 12 gave 702.0 and
-// 702.7 against 701.0 Msamples/s one at a time; 6 and 8 gave 696.5 and 696.8)
+// 702.7 against 701.0 Msamples/s one at a time; 6 and 8 gave 696.5 and 696.8.
+// With instances entered from the top-level step and 9 closest-hit blocks,
+// 10 closest-hit lanes measured 748.3 against 746.2 for 12, and 8 748.1)
 #ifndef PYRE_LEAF_WAIT_CLOSEST
-#define PYRE_LEAF_WAIT_CLOSEST 12
+#define PYRE_LEAF_WAIT_CLOSEST 10
 #endif
 #ifndef PYRE_LEAF_WAIT_ANY
 #define PYRE_LEAF_WAIT_ANY 16
@@ -182,7 +184,7 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 // With WIDTH 4 or 8 the instance BVHs are wide: a node step tests every
 // child box, continues with the nearest hit child and pushes the others
 // farthest first; leaf children are parked when they are reached.
-// Inner nodes are stepped while more than 12 (closest hit) or 16 (any hit)
+// Inner nodes are stepped while more than 10 (closest hit) or 16 (any hit)
 // lanes of the warp
 // still need a leaf (or no lane holds one); a lane that already holds one
 // leaf keeps stepping speculatively. Leaves found on the way are parked (at

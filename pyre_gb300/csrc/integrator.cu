@@ -33,10 +33,11 @@ namespace pyre {
 
 #define PYRE_MAX_DEPTH 64
 // resident blocks of 128 threads per SM for closest-hit (extend, ray queries) and any-hit (shadow) traversal
-// (closest hit: 10 blocks at 48 registers measured 705.9 against 703.5
-// Msamples/s for 9; any hit keeps 9: 10 took 38.5 against 36.5 ms of shadow)
+// (with instances entered from the top-level step, 9 closest-hit blocks
+// measured 746.2 against 737.9 Msamples/s for 10 and 743.4 for 8; any hit at
+// 10 blocks took 36.0 against 34.5 ms of shadow)
 #ifndef PYRE_TRACE_BLOCKS
-#define PYRE_TRACE_BLOCKS 10
+#define PYRE_TRACE_BLOCKS 9
 #endif
 #ifndef PYRE_TRACE_BLOCKS_ANY
 #define PYRE_TRACE_BLOCKS_ANY 9
@@ -338,11 +339,10 @@ struct ExtendRays {
     }
 };
 
-// The traversal kernels are persistent grids of resident 128-thread blocks:
-// 10 per SM for closest hit (48 registers, about 100 bytes of spills) and 9
-// for any hit (56 registers, no spills). Warps wait mostly on node, triangle
-// and stack loads, so more of them per SM pay, up to where the spills cost
-// more than the extra warps hide.
+// The traversal kernels are persistent grids of resident 128-thread blocks,
+// 9 per SM (56 registers). Warps wait mostly on node, triangle and stack
+// loads, so more of them per SM pay, up to where the spills that a smaller
+// register budget forces cost more than the extra warps hide.
 template <bool BATCH, int WIDTH>
 __global__ void __launch_bounds__(128, PYRE_TRACE_BLOCKS) k_extend(DevScene S, PathSoA P, WaveParams W, uint32_t depth) {
     ExtendRays<BATCH> src{&S, &P, &W, depth == 0 ? nullptr : P.q[depth & 1], depth};
