@@ -114,10 +114,12 @@ struct TraceHit {
 // Node steps a lane takes between two warp votes of the inner phase. Each
 // vote (a ballot, a population count and an any) costs issue slots; taking
 // two steps per vote measured 701.8 against 681.0 Msamples/s on the 1080p
-// studio frame (extend 104.0 against 109.4 ms), three 700.6. Films are
-// bit-identical for every setting.
+// studio frame (extend 104.0 against 109.4 ms), three 700.6. With instances
+// entered from the top-level step, three measured 751.3 against 746.4 for
+// two (extend 93.9 against 94.9 ms). Films are bit-identical for every
+// setting.
 #ifndef PYRE_STEPS_PER_VOTE
-#define PYRE_STEPS_PER_VOTE 2
+#define PYRE_STEPS_PER_VOTE 3
 #endif
 
 // Rust-order slab test (bvh.rs:146-153): t1/t2 per axis, max of mins vs
