@@ -235,8 +235,17 @@ def extra_microbench(reps: int = 3) -> dict:
     occ = torch.empty(n, dtype=torch.uint8, device="cuda")
     hits = N.Hits(N.dptr(out["kind"], C.c_int32), N.dptr(out["inst"], C.c_int32), N.dptr(out["tri"], C.c_int32),
                   N.dptr(out["t"]), N.dptr(out["u"]), N.dptr(out["v"]))
+    # the same rays and results in pinned host memory, for the end-to-end calls
+    pin = {k: torch.from_numpy(v).pin_memory() for k, v in (("o", org), ("d", d), ("tmin", tmin), ("tmax", tmax))}
+    hrays = N.Rays(N.dptr(pin["o"]), N.dptr(pin["d"]), N.dptr(pin["tmin"]), N.dptr(pin["tmax"]), None)
+    hout = {k: torch.empty(n, dtype=torch.int32, pin_memory=True) for k in ("kind", "inst", "tri")}
+    hout.update({k: torch.empty(n, dtype=torch.float32, pin_memory=True) for k in ("t", "u", "v")})
+    hocc = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    hhits = N.Hits(N.dptr(hout["kind"], C.c_int32), N.dptr(hout["inst"], C.c_int32), N.dptr(hout["tri"], C.c_int32),
+                   N.dptr(hout["t"]), N.dptr(hout["u"]), N.dptr(hout["v"]))
     res = {"workload": "displaced icosphere level 8 (1,310,720 triangles), 16,777,216 rays from seed 1, "
-                       "t_min 1e-4, t_max inf", "rays": n, "triangles": int(mesh.triangle_count())}
+                       "t_min 1e-4, t_max inf", "rays": n, "triangles": int(mesh.triangle_count()),
+           "e2e": "rays in and results out through the C ABI from / to pinned host memory, copies in the timed call"}
     for q in ("closest", "any"):
         def call():
             if q == "closest":
@@ -250,11 +259,21 @@ def extra_microbench(reps: int = 3) -> dict:
         ms = sorted(call() for _ in range(reps))[reps // 2]
         res[f"{q}_grays_per_s"] = n / ms / 1e6
         res[f"{q}_ms"] = ms
-        # end to end through the Python API: host arrays in and out
-        ctx.intersect(ds, org, d, tmin, tmax, any_hit=(q == "any"))
-        t0 = time.perf_counter()
-        ctx.intersect(ds, org, d, tmin, tmax, any_hit=(q == "any"))
-        res[f"{q}_e2e_grays_per_s"] = n / (time.perf_counter() - t0) / 1e9
+        # end to end through the C ABI: rays from pinned host memory in, results to pinned host memory out
+        def host_call():
+            if q == "closest":
+                ctx.check(ctx.lib.pyre_intersect_closest(ctx.handle, ds.handle, C.byref(hrays), n, C.byref(hhits),
+                                                         N.PYRE_MEM_HOST))
+            else:
+                ctx.check(ctx.lib.pyre_intersect_any(ctx.handle, ds.handle, C.byref(hrays), n,
+                                                     N.dptr(hocc, C.c_uint8), N.PYRE_MEM_HOST))
+        host_call()
+        wall = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            host_call()
+            wall.append(time.perf_counter() - t0)
+        res[f"{q}_e2e_grays_per_s"] = n / sorted(wall)[reps // 2] / 1e9
     res["gpu_launches"] = 2 * reps
     ds.close()
     ctx.close()

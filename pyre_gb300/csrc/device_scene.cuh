@@ -116,11 +116,25 @@ struct TraceHit {
 // two steps per vote measured 701.8 against 681.0 Msamples/s on the 1080p
 // studio frame (extend 104.0 against 109.4 ms), three 700.6. With instances
 // entered from the top-level step, three measured 751.3 against 746.4 for
-// two (extend 93.9 against 94.9 ms). Films are bit-identical for every
-// setting.
+// two (extend 93.9 against 94.9 ms); with 256-bit node loads, four measured
+// 768.5 against 763.4 for three. Films are bit-identical for every setting.
 #ifndef PYRE_STEPS_PER_VOTE
-#define PYRE_STEPS_PER_VOTE 3
+#define PYRE_STEPS_PER_VOTE 4
 #endif
+
+// Binary node fetch: one 64-B node as two 256-bit loads (sm_100+ `ld.v8`;
+// nodes are 64-B aligned) instead of four 128-bit ones, so a node step issues
+// two load instructions. The traversal is issue-bound: 763.4 against 749.8
+// Msamples/s on the 1080p studio frame (extend 92.1 against 94.0 ms, shadow
+// 33.2 against 34.5 ms), films bit-identical.
+#ifndef PYRE_LD256
+#define PYRE_LD256 1
+#endif
+__device__ __forceinline__ void ldg_256(const float4* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
 
 // Rust-order slab test (bvh.rs:146-153): t1/t2 per axis, max of mins vs
 // t_min, min of maxes vs t_max, hit iff tmin <= tmax. Returns the entry.
@@ -424,8 +438,16 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                     continue;
                 }
                 const float4* N = S.nodes + 4 * (size_t)(node & ~PYRE_TAG_TOP);
+#if PYRE_LD256
+                float4 na, nb, nc, ndf;
+                ldg_256(N, na, nb);
+                ldg_256(N + 2, nc, ndf);
+                const int4 nd = make_int4(__float_as_int(ndf.x), __float_as_int(ndf.y), __float_as_int(ndf.z),
+                                          __float_as_int(ndf.w));
+#else
                 const float4 na = __ldg(N), nb = __ldg(N + 1), nc = __ldg(N + 2);
                 const int4 nd = __ldg(reinterpret_cast<const int4*>(N + 3));
+#endif
                 float e0, e1;
                 const bool h0 = nd.x >= 0 && slab(na.x, na.y, na.z, na.w, nc.x, nc.y, o, inv, r.tmin, best_t, &e0);
                 const bool h1 = nd.y >= 0 && slab(nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, o, inv, r.tmin, best_t, &e1);
