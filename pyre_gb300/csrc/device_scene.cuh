@@ -89,6 +89,7 @@ struct DevScene {
 struct TraceRay {
     f3 o, d;
     float tmin, tmax, time;
+    uint32_t job;  // batched rendering: the ray's job (set and read by the ray source only)
 };
 
 struct TraceHit {
@@ -262,7 +263,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
     bool active = false;    // the lane holds a ray
     uint32_t id = 0;
     TraceRay r;
-    r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.tmin = 0.0f; r.tmax = 0.0f; r.time = 0.0f;
+    r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.tmin = 0.0f; r.tmax = 0.0f; r.time = 0.0f; r.job = 0;
     TraceHit hit;
     hit.inst = -1; hit.tri = -1; hit.light = -1; hit.t = 0.0f; hit.u = 0.0f; hit.v = 0.0f;
     f3 inv = splat3(0.0f);

@@ -147,7 +147,7 @@ struct PathSoA {
     float4* acc_a;     // albedo sum
     float4* acc_n;     // normal sum
     WaveCtl* ctl;
-    uint32_t* pjob;    // batch: job of each path
+    int32_t* sroot;    // batch: per shadow-queue entry, the top-level root of the ray's job
     // adjoint replay (null otherwise)
     float4* keep_L;    // per (sample, pixel) of the sample range: final path radiance (pyre_forward)
     float4* gpend;     // 3 per NEE slot: parked gradient terms of that slot
@@ -232,7 +232,7 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
     const uint32_t n = P.ctl->n_valid;
     const uint32_t s_base = P.ctl->s_base;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t x, y, s, width, height, max_depth = W.max_depth;
+        uint32_t x, y, s, width, height, max_depth = W.max_depth, job = 0;
         const DevCamera* cam = &W.cam;
         if (BATCH) {
             const DevWave& wv = W.waves[P.ctl->wave];
@@ -243,7 +243,7 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
             width = J.width; height = J.height;
             max_depth = J.max_depth;
             cam = &J.cam;
-            P.pjob[i] = sg.job;
+            job = sg.job;
         } else {
             const uint32_t k = i / W.npix, p = i - k * W.npix;
             x = W.cx0 + p % W.cw; y = W.cy0 + p / W.cw; s = s_base + k;
@@ -259,7 +259,8 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
         float time = g.next_f32();
         f3 o, d;
         camera_ray(*cam, ndc, lens, &o, &d);
-        __stcs(&P.ray_o[0][i], make_float4(o.x, o.y, o.z, 1e-4f));
+        // a batch ray carries its job in the origin's w (the traversal's t_min is a constant)
+        __stcs(&P.ray_o[0][i], make_float4(o.x, o.y, o.z, BATCH ? __uint_as_float(job) : 1e-4f));
         __stcs(&P.ray_d[0][i], make_float4(d.x, d.y, d.z, time));
         store_rng(P.rng, i, g);
         // radiance 0, throughput 1 and the AOVs are set by shade at depth 0;
@@ -324,13 +325,14 @@ struct ExtendRays {
         r.tmin = 1e-4f;
         r.tmax = __int_as_float(0x7f800000);
         r.time = rd.w;
-        root = BATCH ? W->jobs[P->pjob[qin ? __ldcs(qin + p) : p]].tlas_root : S->tlas_root;
+        r.job = BATCH ? __float_as_uint(ro.w) : 0u;  // batch: the ray's job
+        root = BATCH ? W->jobs[r.job].tlas_root : S->tlas_root;
         return p;
     }
     __device__ __forceinline__ void store(uint32_t p, const TraceRay& r, TraceHit& h, bool) const {
         uint32_t lfirst = 0, lcount = S->n_lights;
         if (BATCH) {
-            const DevJob& J = W->jobs[P->pjob[qin ? __ldcs(qin + p) : p]];
+            const DevJob& J = W->jobs[r.job];
             lfirst = J.light_first; lcount = J.light_count;
         }
         hit_quad_lights(*S, r, lfirst, lcount, &h);
@@ -366,7 +368,7 @@ struct ShadowRays {
         r.tmin = 1e-3f;
         r.tmax = so.w;
         r.time = sd.w;
-        root = BATCH ? W->jobs[P->pjob[target / W->ns]].tlas_root : S->tlas_root;
+        root = BATCH ? __ldcs(P->sroot + j) : S->tlas_root;
         return target;
     }
     __device__ __forceinline__ void store(uint32_t target, const TraceRay&, TraceHit&, bool occluded) const {
@@ -497,8 +499,12 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
         // queue position of the path's ray and hit (depth 0: the path index), and the path
         const uint32_t pos = W.sort ? P.qsort[j] : (depth > 0 ? j : (BATCH ? j : tiled_path(W, j)));
         const uint32_t i = depth > 0 ? __ldcs(qin + pos) : pos;
+        // a batch ray carries its job in the origin's w
+        float4 ro_b = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (BATCH) ro_b = __ldcs(P.ray_o[depth & 1] + pos);
+        const DevJob* JB = BATCH ? &W.jobs[__float_as_uint(ro_b.w)] : nullptr;
         // a batch wave traces every job's camera rays; a job with max_depth 0 shades none
-        if (BATCH && depth == 0 && W.jobs[P.pjob[i]].max_depth == 0) continue;
+        if (BATCH && depth == 0 && JB->max_depth == 0) continue;
         // a camera path starts with radiance 0 and throughput 1 (integrator.rs:63-64)
         const float4 Lq = depth > 0 ? __ldcs(P.L + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         f3 L = mk3(Lq.x, Lq.y, Lq.z);
@@ -543,7 +549,7 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
         const float4 bq = depth > 0 ? __ldcs(P.beta + i) : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         f3 beta = mk3(bq.x, bq.y, bq.z);
         const float last_pdf = bq.w;
-        const float4 ro = __ldcs(P.ray_o[depth & 1] + pos), rd = __ldcs(P.ray_d[depth & 1] + pos);
+        const float4 ro = BATCH ? ro_b : __ldcs(P.ray_o[depth & 1] + pos), rd = __ldcs(P.ray_d[depth & 1] + pos);
         const f3 ray_o = mk3(ro.x, ro.y, ro.z), ray_d = mk3(rd.x, rd.y, rd.z);
         const float time = rd.w;
         const float4 hq = __ldcs(P.hit + pos);
@@ -621,8 +627,7 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
                 const f3 p_off = p + 1e-3f * ns;
                 uint32_t lfirst = 0, lcount = S.n_lights;
                 if (BATCH) {
-                    const DevJob& J = W.jobs[P.pjob[i]];
-                    lfirst = J.light_first; lcount = J.light_count;
+                    lfirst = JB->light_first; lcount = JB->light_count;
                 }
                 // The vertex's sampling arms in the reference's order, each
                 // drawing its two numbers first: NEE for every quad light
@@ -670,7 +675,7 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
                         if (cos_wi == 0.0f) break;
                         beta = beta * (f * cos_wi / pdf_b);
                         bool survive = true;
-                        if (depth >= (BATCH ? W.jobs[P.pjob[i]].min_rr : W.min_rr)) {
+                        if (depth >= (BATCH ? JB->min_rr : W.min_rr)) {
                             float q = clampf_(1.0f - max_elem3(beta), 0.05f, 0.95f);
                             if (g.next_f32() < q) survive = false;
                             else beta = beta / (1.0f - q);
@@ -678,11 +683,12 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
                         if (survive) {
                             // Next ray (integrator.rs:377-387), at the path's
                             // position in the next depth's queue
-                            if (depth + 1 < (BATCH ? W.jobs[P.pjob[i]].max_depth : W.max_depth)) {
+                            if (depth + 1 < (BATCH ? JB->max_depth : W.max_depth)) {
                                 const f3 nd = to_world(fr, wi);
                                 const uint32_t q = append_slot(next_count);
                                 qout[q] = i;
-                                __stcs(P.ray_o[(depth + 1) & 1] + q, make_float4(p_off.x, p_off.y, p_off.z, 1e-4f));
+                                __stcs(P.ray_o[(depth + 1) & 1] + q,
+                                       make_float4(p_off.x, p_off.y, p_off.z, BATCH ? ro.w : 1e-4f));
                                 __stcs(P.ray_d[(depth + 1) & 1] + q, make_float4(nd.x, nd.y, nd.z, time));
                             }
                             __stcs(P.beta + i, make_float4(beta.x, beta.y, beta.z, pdf_b));
@@ -702,12 +708,15 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
                     if (ADJ) {  // park the slot's d/d params (and texels); cleared if occluded
                         float4* G = P.gpend + PYRE_GSLOT * sidx;
                         float gm[6];
-                        if (!env_arm) {  // beta * f * (Le cos w / pdf)
-                            jac_dot(mat, wo, wi, delta * beta * (le * wi.z * w / lpdf), gm);
+                        // quad light: beta * f * (Le cos w / pdf); environment:
+                        // beta * f * (texture * intensity) * k, k = cos w / pdf.
+                        // One Jacobian call site for both arms keeps the kernel's
+                        // code (and its instruction-cache misses) smaller.
+                        const float k = wi.z * w / lpdf;
+                        jac_dot(mat, wo, wi, delta * beta * (env_arm ? le * k : le * wi.z * w / lpdf), gm);
+                        if (!env_arm) {
                             G[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                        } else {  // beta * f * (texture * intensity) * k, k = cos w / pdf
-                            const float k = wi.z * w / lpdf;
-                            jac_dot(mat, wo, wi, delta * beta * (le * k), gm);
+                        } else {
                             const f2 uv = env_dir_to_uv(wi_w);
                             const f3 ke = delta * beta * f * k;
                             G[2] = make_float4(uv.x, uv.y, 1.0f, 0.0f);
@@ -721,6 +730,7 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
                         __stcs(P.sh_o + q, make_float4(p_off.x, p_off.y, p_off.z, sh_tmax));
                         __stcs(P.sh_d + q, make_float4(sh_dir.x, sh_dir.y, sh_dir.z, time));
                         P.sq[q] = (uint32_t)sidx;
+                        if (BATCH) __stcs(P.sroot + q, JB->tlas_root);
                     }
                 }
                 store_rng(P.rng, i, g);
@@ -796,13 +806,13 @@ __global__ void k_accumulate_batch(PathSoA P, WaveParams W) {
         float4 ar = P.acc_r[a], aa = P.acc_a[a], an = P.acc_n[a];
         for (uint32_t k = 0; k < sg.s_count; ++k) {
             const uint32_t i = sg.path_base + k * J.npix + p;
-            float4 Lq = P.L[i];
+            const float4 Lq = __ldcs(P.L + i);  // last reads of the path state
             f3 L = mk3(Lq.x, Lq.y, Lq.z);
             for (uint32_t s = 0; s < W.ns; ++s) {
-                float4 c = P.pend[(size_t)i * W.ns + s];
+                const float4 c = __ldcs(P.pend + (size_t)i * W.ns + s);
                 if (c.w != 0.0f) L = L + mk3(c.x, c.y, c.z);
             }
-            float4 al = P.aov_a[i], nn = P.aov_n[i];
+            const float4 al = __ldcs(P.aov_a + i), nn = __ldcs(P.aov_n + i);
             ar.x += L.x; ar.y += L.y; ar.z += L.z; ar.w += al.w;
             aa.x += al.x; aa.y += al.y; aa.z += al.z;
             an.x += nn.x; an.y += nn.y; an.z += nn.z;
@@ -936,7 +946,7 @@ size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* ou
     s.acc_a = c.take<float4>(npix);
     s.acc_n = c.take<float4>(npix);
     s.ctl = c.take<WaveCtl>(1);
-    s.pjob = batch ? c.take<uint32_t>(P) : nullptr;
+    s.sroot = batch ? c.take<int32_t>(P * ns) : nullptr;
     s.keep_L = nullptr;
     s.gpend = adjoint ? c.take<float4>(P * ns * PYRE_GSLOT) : nullptr;
     s.brec = adjoint ? c.take<float4>(3 * P) : nullptr;
