@@ -269,7 +269,7 @@ typedef struct pyre_render_params {
     uint32_t sort_by_material;       /* reorder the shade queue by material */
     uint32_t use_graph;              /* capture one wave as a CUDA graph and replay it */
     uint32_t refill_lanes;           /* traversal: refetch rays once this many lanes of a
-                                        warp are idle (1-32); 0 = 16 for closest hit,
+                                        warp are idle (1-32); 0 = 12 for closest hit,
                                         8 for any hit */
     uint32_t bvh_width;              /* instance BVH width 2, 4 or 8; 0 = the scene's
                                         (pyre_scene_set_bvh_width) */

@@ -26,7 +26,7 @@ KNOBS = {
     "use_graph": [0, 1],
     "bvh_width": [2, 4, 8],
     "sort_by_material": [0, 1],
-    "refill_lanes": [0, 4, 8, 16, 32],  # 0: the library's defaults (16 closest hit, 8 any hit)
+    "refill_lanes": [0, 4, 8, 16, 32],  # 0: the library's defaults (12 closest hit, 8 any hit)
 }
 DEFAULT = {"wave_paths": 0, "block_size": 0, "use_graph": 0, "bvh_width": 2, "sort_by_material": 0,
            "refill_lanes": 0}

@@ -105,9 +105,11 @@ struct TraceHit {
 // (with two node steps per vote: 12 and 16 against 8 and 12 gave 702.0 and
 // 702.7 against 701.0 Msamples/s one at a time; 6 and 8 gave 696.5 and 696.8.
 // With instances entered from the top-level step and 9 closest-hit blocks,
-// 10 closest-hit lanes measured 748.3 against 746.2 for 12, and 8 748.1)
+// 10 closest-hit lanes measured 748.3 against 746.2 for 12, and 8 748.1.
+// Once closest-hit lanes stopped at their first leaf, 16 lanes measured
+// 758.8 against 755.6 for 10, 750.7 for 20 and 741.1 for 24)
 #ifndef PYRE_LEAF_WAIT_CLOSEST
-#define PYRE_LEAF_WAIT_CLOSEST 10
+#define PYRE_LEAF_WAIT_CLOSEST 16
 #endif
 #ifndef PYRE_LEAF_WAIT_ANY
 #define PYRE_LEAF_WAIT_ANY 16
@@ -201,10 +203,10 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 // With WIDTH 4 or 8 the instance BVHs are wide: a node step tests every
 // child box, continues with the nearest hit child and pushes the others
 // farthest first; leaf children are parked when they are reached.
-// Inner nodes are stepped while more than 10 (closest hit) or 16 (any hit)
-// lanes of the warp
-// still need a leaf (or no lane holds one); a lane that already holds one
-// leaf keeps stepping speculatively. Leaves found on the way are parked (at
+// Inner nodes are stepped while more than 16 lanes of the warp still need a
+// leaf (or no lane holds one); an any-hit lane that already holds one leaf
+// keeps stepping speculatively, a closest-hit lane waits for the leaf phase
+// (see STOP). Leaves found on the way are parked (at
 // most three triangle ranges, all of the current instance: a lane holding
 // leaves does not leave or enter an instance) and then tested by all lanes in
 // lock step. An any-hit lane that finds a hit is finished at the end of that
@@ -252,9 +254,17 @@ __device__ __forceinline__ void sort_children(float (&e)[W], int (&c)[W]) {
 template <bool ANY, int WIDTH, class Src>
 __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, uint32_t n, uint32_t* counter,
                                              int refill) {
-    // a lane stops stepping nodes once it holds STOP parked leaves (a binary
-    // step can park two, a wide step at most one)
-    constexpr int STOP = WIDTH > 2 ? 3 : 2;
+    // A lane stops stepping nodes once it holds STOP parked leaves (a binary
+    // step can park two, a wide step at most one). A closest-hit lane stops
+    // at its first: its leaves are then tested before its next node step, so
+    // the boxes it culls with its current closest distance, and its hit, do
+    // not depend on the other lanes of its warp. Where two triangles are hit
+    // at distances a rounding apart, a box whose rounded entry lies between
+    // them is culled or not depending on when the nearer hit was recorded;
+    // with speculative steps that point moved with the warp, and about one
+    // pixel in 10^6 of 1024^2 Cornell views changed from run to run. Any hit
+    // culls with the ray's own fixed t_max, so its lanes keep stepping.
+    constexpr int STOP = ANY ? (WIDTH > 2 ? 3 : 2) : 1;
     constexpr int LEAF_WAIT = ANY ? PYRE_LEAF_WAIT_ANY : PYRE_LEAF_WAIT_CLOSEST;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
