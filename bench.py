@@ -314,7 +314,7 @@ def extra_adjoint(reps: int = 3) -> dict:
             "e2e_step_ms": 1e3 * float(np.median(wall))}
 
 
-def extra_batch(reps: int = 1) -> dict:
+def extra_batch(reps: int = 3) -> dict:
     """256 batched jobs (Cornell variants with 10..200k-triangle inserts, 128^2..1024^2, 4/16/64 spp, depth
     4-12) against one pyre_render per job. Both arms write the same caller-owned host films and are timed on the
     wall clock (e2e: every launch, host gap, film copy and synchronisation) and by the library's CUDA events
@@ -365,9 +365,11 @@ def extra_batch(reps: int = 1) -> dict:
         return wall, dev, n
 
     batched()
-    b = sorted(batched() for _ in range(reps))[reps // 2]
+    with Clocks(0) as clk_b:
+        b = sorted(batched() for _ in range(reps))[reps // 2]
     per_view()
-    v = sorted(per_view()[:2] for _ in range(reps))[reps // 2]
+    with Clocks(0) as clk_v:
+        v = sorted(per_view()[:2] for _ in range(reps))[reps // 2]
     # per-view cost by image size: where the samples and the time are
     by_size = {}
     for k, j in enumerate(jobs):
@@ -388,10 +390,14 @@ def extra_batch(reps: int = 1) -> dict:
     sspec = [dict(spec[k], part=i) for i, k in enumerate(small_idx)]
     sfilms = [films[k] for k in small_idx]
     sub.render_batch(dsub, sspec, use_graph=1, films=sfilms)
-    t0 = time.perf_counter()
-    sub.render_batch(dsub, sspec, use_graph=1, films=sfilms)
-    sb_wall, sb_dev = time.perf_counter() - t0, sub.stats().ms_total / 1e3
-    sv_wall, sv_dev, s_samples = per_view(small_only=True)
+
+    def small_batched():
+        t0 = time.perf_counter()
+        sub.render_batch(dsub, sspec, use_graph=1, films=sfilms)
+        return time.perf_counter() - t0, sub.stats().ms_total / 1e3
+
+    sb_wall, sb_dev = sorted(small_batched() for _ in range(reps))[reps // 2]
+    sv_wall, sv_dev, s_samples = sorted(per_view(small_only=True) for _ in range(reps))[reps // 2]
     dsub.close()
     sub.close()
     for s1 in singles:
@@ -404,6 +410,7 @@ def extra_batch(reps: int = 1) -> dict:
             "per_view_e2e_msamples_per_s": samples / v[0] / 1e6, "per_view_device_msamples_per_s": samples / v[1] / 1e6,
             "batched_over_per_view_e2e": v[0] / b[0], "batched_over_per_view_device": v[1] / b[1],
             "per_view_by_size": dict(sorted(by_size.items(), key=lambda kv: int(kv[0].split("^")[0]))),
+            "clocks": {"batched": clk_b.summary(), "per_view": clk_v.summary()},
             "small_jobs": {"jobs": len(small_idx), "samples": s_samples,
                            "batched_over_per_view_e2e": sv_wall / sb_wall,
                            "batched_over_per_view_device": sv_dev / sb_dev}}
@@ -479,8 +486,10 @@ class Clocks:
             for k, nm in enumerate(names):
                 if len(r) > 5 + k and r[5 + k] == "Active":
                     reasons.add(nm)
+        pw = [float(r[3]) for r in self.rows if len(r) > 3 and r[3].replace(".", "").isdigit()]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.rows)}
+                "reasons": sorted(reasons), "samples": len(self.rows),
+                "power_w": statistics.median(pw) if pw else None}
 
 
 def make_workload():

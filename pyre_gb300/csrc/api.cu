@@ -225,9 +225,15 @@ __global__ void k_dist2d_query(DevEnv E, int cdf_mode, const float* __restrict__
 // index[index_base(mesh) + 3 * local id], the local id being the triangle
 // record's .w. Slots run mesh by mesh; mesh k holds slots
 // [slot_start[k], slot_start[k + 1]).
-__global__ void k_slot_index(const float4* __restrict__ tris, const uint32_t* __restrict__ index,
-                             const uint32_t* __restrict__ slot_start, const uint32_t* __restrict__ index_base,
-                             uint32_t n_mesh, uint32_t n_slots, uint4* __restrict__ out) {
+// The three vertex normals of each triangle slot, in BVH leaf order (zero for
+// meshes without normals, whose shading normal comes from the edges): shade
+// reads a hit's normals with three loads from one 48-B record that does not
+// wait for the instance, instead of a vertex-id record and nine loads that
+// wait on it (shade 43.5 against 44.7 ms on the 1080p studio frame).
+__global__ void k_slot_normals(const float4* __restrict__ tris, const uint32_t* __restrict__ index,
+                               const float* __restrict__ normal, const uint32_t* __restrict__ slot_start,
+                               const uint32_t* __restrict__ index_base, const uint8_t* __restrict__ has_normals,
+                               uint32_t n_mesh, uint32_t n_slots, float4* __restrict__ out) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_slots; t += gridDim.x * blockDim.x) {
         uint32_t lo = 0, hi = n_mesh - 1;  // last mesh with slot_start <= t
         while (lo < hi) {
@@ -235,7 +241,14 @@ __global__ void k_slot_index(const float4* __restrict__ tris, const uint32_t* __
             if (slot_start[mid] <= t) lo = mid; else hi = mid - 1;
         }
         const size_t row = index_base[lo] + 3 * (size_t)__float_as_uint(tris[3 * (size_t)t].w);
-        out[t] = make_uint4(index[row], index[row + 1], index[row + 2], 0u);
+        for (int k = 0; k < 3; ++k) {
+            float4 n = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (has_normals[lo]) {
+                const size_t a = 3 * (size_t)index[row + k];
+                n = make_float4(normal[a], normal[a + 1], normal[a + 2], 0.0f);
+            }
+            out[3 * (size_t)t + k] = n;
+        }
     }
 }
 
@@ -628,35 +641,38 @@ static int upload_parts(pyre_ctx* ctx, const pyre_scene_desc* desc, const std::v
     float* d_normal = nullptr;
     if ((rc = upload(ctx, sc, normal, &d_normal)) != PYRE_OK) return fail(rc);
     D.normal = d_normal;
-    // the vertex ids of each triangle slot, so that shade reads a hit's
-    // normals without waiting for its instance and triangle record
-    D.slot_index = nullptr;
+    // the vertex normals of each triangle slot (k_slot_normals)
+    D.slot_normals = nullptr;
     if (total_tris) {
         std::vector<uint32_t> slot_start, index_base;
+        std::vector<uint8_t> has_normals;
         uint32_t acc = 0;
         for (uint32_t m = 0; m < n_meshes; ++m) {
             if (desc->meshes[m].n_triangles == 0) continue;
             slot_start.push_back(acc);
             index_base.push_back((uint32_t)mesh_index_base[m]);
+            has_normals.push_back(mesh_normal_base[m] >= 0 ? 1 : 0);
             acc += desc->meshes[m].n_triangles;
         }
         uint32_t *d_start = nullptr, *d_base = nullptr;
+        uint8_t* d_has = nullptr;
         if ((rc = upload(ctx, sc, slot_start, &d_start)) != PYRE_OK) return fail(rc);
         if ((rc = upload(ctx, sc, index_base, &d_base)) != PYRE_OK) return fail(rc);
+        if ((rc = upload(ctx, sc, has_normals, &d_has)) != PYRE_OK) return fail(rc);
         void* p = nullptr;
         if (injected_alloc_failure(ctx))
             return fail(set_error(ctx, PYRE_ERR_OOM, "cudaMalloc(scene): injected allocation failure"));
-        cudaError_t e = cudaMalloc(&p, (size_t)total_tris * sizeof(uint4));
+        cudaError_t e = cudaMalloc(&p, (size_t)total_tris * 3 * sizeof(float4));
         if (e != cudaSuccess) { cudaGetLastError(); return fail(cuda_check(ctx, e, "cudaMalloc(scene)")); }
         sc->allocations.push_back(p);
-        sc->device_bytes += (size_t)total_tris * sizeof(uint4);
+        sc->device_bytes += (size_t)total_tris * 3 * sizeof(float4);
         const uint32_t grid = (uint32_t)std::min<uint64_t>((total_tris + 255) / 256, 65535);
-        k_slot_index<<<grid, 256>>>(d_tris, d_index, d_start, d_base, (uint32_t)slot_start.size(),
-                                    (uint32_t)total_tris, (uint4*)p);
+        k_slot_normals<<<grid, 256>>>(d_tris, d_index, d_normal, d_start, d_base, d_has, (uint32_t)slot_start.size(),
+                                      (uint32_t)total_tris, (float4*)p);
         e = cudaDeviceSynchronize();
         if (e == cudaSuccess) e = cudaGetLastError();
-        if (e != cudaSuccess) return fail(cuda_check(ctx, e, "slot index"));
-        D.slot_index = (const uint4*)p;
+        if (e != cudaSuccess) return fail(cuda_check(ctx, e, "slot normals"));
+        D.slot_normals = (const float4*)p;
     }
     DevMaterial* d_mats = nullptr;
     if ((rc = upload(ctx, sc, mats, &d_mats)) != PYRE_OK) return fail(rc);

@@ -9,7 +9,7 @@
 //                       moller_trumbore computes them (mesh.rs:153-157)
 //   inst   DevInstance[] instances in top-level-leaf order
 //   index  uint32[3*T]  mesh index buffers rebased to global vertex ids
-//   slot_index uint4[T] per triangle slot, its row of `index` (for shading)
+//   slot_normals float4[3*T] per triangle slot, its three vertex normals (for shading)
 //   normal float[3*V]   vertex normals (meshes without normals use e1 x e2)
 #pragma once
 #include <cuda_runtime.h>
@@ -67,7 +67,7 @@ struct DevScene {
     int32_t tlas_root;     // -1: no geometry
     const uint32_t* index;
     const float* normal;
-    const uint4* slot_index;  // per triangle slot: the triangle's row of `index` (x, y, z)
+    const float4* slot_normals;  // 3 per triangle slot: its vertex normals (xyz, 0)
     const DevMaterial* materials;
     uint32_t n_materials;
     const DevQuadLight* lights;

@@ -605,13 +605,12 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
             f3 o_local = moved ? ray_o - off : ray_o;
             f3 p = o_local + ray_d * t;
             if (moved) p = p + off;
-            const uint4 vx = __ldg(S.slot_index + slot);  // does not wait for the instance
             f3 ns;
+            // the slot's vertex normals: one record, does not wait for the instance
+            const float4 n0 = __ldg(S.slot_normals + 3 * (size_t)slot), n1 = __ldg(S.slot_normals + 3 * (size_t)slot + 1),
+                         n2 = __ldg(S.slot_normals + 3 * (size_t)slot + 2);
             if (I.normal_base >= 0) {
-                const uint32_t a = vx.x, b = vx.y, c = vx.z;
-                const f3 na = mk3(S.normal[3 * (size_t)a], S.normal[3 * (size_t)a + 1], S.normal[3 * (size_t)a + 2]);
-                const f3 nb = mk3(S.normal[3 * (size_t)b], S.normal[3 * (size_t)b + 1], S.normal[3 * (size_t)b + 2]);
-                const f3 nc = mk3(S.normal[3 * (size_t)c], S.normal[3 * (size_t)c + 1], S.normal[3 * (size_t)c + 2]);
+                const f3 na = mk3(n0.x, n0.y, n0.z), nb = mk3(n1.x, n1.y, n1.z), nc = mk3(n2.x, n2.y, n2.z);
                 const float w = 1.0f - u - v;
                 ns = normalize3(w * na + u * nb + v * nc);
             } else {
