@@ -223,9 +223,6 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 #define PYRE_NODE_NONE (-1)
 // top-level leaves of one static instance are entered from the top-level
 // step (INST|TOP entries); 0 keeps every instance behind an INST entry
-#ifndef PYRE_ANY_UNORDERED
-#define PYRE_ANY_UNORDERED 0
-#endif
 #ifndef PYRE_TLAS_ENTER
 #define PYRE_TLAS_ENTER 1
 #endif
@@ -489,7 +486,7 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                 const int tag = top ? PYRE_TAG_TOP : 0;
                 const bool g0 = h0 && !leaf0, g1 = h1 && !leaf1;
                 if (g0 && g1) {
-                    const bool first0 = (ANY && PYRE_ANY_UNORDERED) ? true : e0 <= e1;
+                    const bool first0 = e0 <= e1;
                     if (sp >= STACK) { atomicExch(S.error_flag, -5); exhausted = true; sp = 0; continue; }
                     spush((first0 ? nd.y : nd.x) | tag);
                     node = (first0 ? nd.x : nd.y) | tag;
