@@ -169,6 +169,9 @@ __device__ __forceinline__ T warp_sum(T v) {
 #endif
 // The same for the material terms when the block sums them in shared memory
 // (FP64): 23.9 against 24.6 ms.
+#ifndef PYRE_MAT_WARP32
+#define PYRE_MAT_WARP32 0
+#endif
 #ifndef PYRE_MAT_DIRECT
 #define PYRE_MAT_DIRECT 1
 #endif
@@ -333,7 +336,11 @@ __device__ __forceinline__ void warp_flush(const DevScene& S, float* env_grad, d
             todo &= ~__ballot_sync(FULL, mine);
 #pragma unroll
             for (int k = 0; k < PYRE_NPARAM; ++k) {
+#if PYRE_MAT_WARP32
+                const double v = (double)warp_sum(mine ? t.g[k] : 0.0f);
+#else
                 const double v = warp_sum(mine ? (double)t.g[k] : 0.0);
+#endif
                 if (lane == src) mat_add(key, k, v);
             }
             if (mine) left = false;
