@@ -167,13 +167,19 @@ __device__ __forceinline__ T warp_sum(T v) {
 #ifndef PYRE_ENV_CACHE_DIRECT
 #define PYRE_ENV_CACHE_DIRECT 1
 #endif
-// The same for the material terms when the block sums them in shared memory
-// (FP64): 23.9 against 24.6 ms.
+// Material terms: lanes that hold the same material (most of a warp once the
+// backward sorts its paths by material) are summed with full-warp FP32
+// butterflies, and one lane adds each sum to the block's FP64 sums in shared
+// memory; other lanes add their own terms. The backward of the 512^2 problem
+// took 19.3 ms, against 19.7 with FP64 butterflies and 20.0 with every lane
+// adding to the FP64 sums (PYRE_MAT_DIRECT; before the material sort that
+// was the fastest: 23.9 against 24.6 ms). A warp sums at most 32 terms in
+// FP32; the sums over the block and the image stay FP64.
 #ifndef PYRE_MAT_WARP32
-#define PYRE_MAT_WARP32 0
+#define PYRE_MAT_WARP32 1
 #endif
 #ifndef PYRE_MAT_DIRECT
-#define PYRE_MAT_DIRECT 1
+#define PYRE_MAT_DIRECT 0
 #endif
 
 // A block's gradient accumulators in its dynamic shared memory: the texel

@@ -87,8 +87,12 @@ def test_backward_uses_forward_tape(gpu_ctx):
     ref = gpu_ctx.render(ds, cam, it, 48, 48, 4, env_sampling=PYRE_ENV_CDF, spp_begin=7)
     np.testing.assert_array_equal(film.radiance, ref.radiance)
     b_m, b_e = gpu_ctx.backward(ds, cam, it, 48, 48, 4, dl, env_sampling=PYRE_ENV_CDF, spp_begin=7)
-    np.testing.assert_allclose(a_m, b_m, rtol=1e-9, atol=1e-12)
-    # Texel gradients sum by FP32 atomics whose order varies run to run.
+    # Material terms are summed per warp in FP32 before the FP64 sums, and
+    # which paths share a warp follows the material-sorted queue, whose order
+    # within a material varies run to run (differences of a few 1e-9 of the
+    # largest gradient, seen on entries that cancel); texel gradients sum by
+    # FP32 atomics whose order varies as well.
+    np.testing.assert_allclose(a_m, b_m, rtol=1e-5, atol=1e-7 * float(np.abs(b_m).max()))
     np.testing.assert_allclose(a_e, b_e, rtol=0, atol=1e-5 * float(np.abs(b_e).max()))
     ds.close()
 
