@@ -55,7 +55,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--graph", type=int, default=0, help="replay waves through a CUDA graph")
     ap.add_argument("--bvh-width", type=int, default=0, help="instance BVH width 2, 4 or 8 (0 = 2)")
-    ap.add_argument("--sort", type=int, default=0, help="shade the live paths sorted by material")
+    ap.add_argument("--sort", type=int, default=1,
+                    help="shade queue order (sort_by_material): 1 = sorted by material within tiles of 2048 "
+                         "entries (the fastest on this frame), 0 = the library default (unsorted), 2 = unsorted, "
+                         "3 = the whole queue sorted")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths in flight per wave (0 = library default)")
     ap.add_argument("--block", type=int, default=0, help="threads per block of the stage kernels (0 = default)")
     ap.add_argument("--refill", type=int, default=0,

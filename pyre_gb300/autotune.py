@@ -25,7 +25,7 @@ KNOBS = {
     "block_size": [0, 128],  # 0: the library's defaults
     "use_graph": [0, 1],
     "bvh_width": [2, 4, 8],
-    "sort_by_material": [0, 1],
+    "sort_by_material": [0, 1, 3],  # 0: the library's default (off), 1: within tiles, 3: the whole queue
     "refill_lanes": [0, 4, 8, 16, 32],  # 0: the library's defaults (12 closest hit, 8 any hit)
 }
 DEFAULT = {"wave_paths": 0, "block_size": 0, "use_graph": 0, "bvh_width": 2, "sort_by_material": 0,

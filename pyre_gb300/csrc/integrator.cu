@@ -43,6 +43,10 @@ namespace pyre {
 #define PYRE_TRACE_BLOCKS_ANY 9
 #endif
 #define PYRE_SORT_BINS 1024  // shade-queue sort keys: escaped, light hit, then materials
+// WaveParams::sort: how shade's queue is ordered by material
+#define PYRE_SORT_OFF 0
+#define PYRE_SORT_TILES 1  // within tiles of PYRE_SORT_TILE_N consecutive entries
+#define PYRE_SORT_QUEUE 2  // the whole queue
 
 struct WaveCtl {
     uint32_t wave;
@@ -123,6 +127,18 @@ static inline int refill_lanes(const pyre_render_params* rp, bool any_hit = fals
     const uint32_t v = rp ? rp->refill_lanes : 0u;
     if (v == 0) return any_hit ? PYRE_DEFAULT_REFILL_ANY : PYRE_DEFAULT_REFILL;
     return (int)std::min<uint32_t>(v, 32u);
+}
+
+// sort_by_material of pyre_render_params: 0 = the call's default, 1 = within
+// tiles, 2 = off, 3 = the whole queue; -1 for any other value.
+int sort_kind(uint32_t v, int dflt) {
+    switch (v) {
+        case 0: return dflt;
+        case 1: return PYRE_SORT_TILES;
+        case 2: return PYRE_SORT_OFF;
+        case 3: return PYRE_SORT_QUEUE;
+        default: return -1;
+    }
 }
 
 #define PYRE_GSLOT 4  // float4s of parked gradient terms per NEE slot
@@ -475,6 +491,68 @@ __global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
         if (lane == leader) base = atomicAdd(&P.ctl->sort_off[key], (uint32_t)__popc(peers));
         base = __shfl_sync(peers, base, leader);
         P.qsort[base + __popc(peers & below)] = j;  // the queue position
+    }
+}
+
+// Material sort within tiles of PYRE_SORT_TILE_N consecutive queue entries:
+// one block sorts a tile by shade key in shared memory (a warp-aggregated
+// histogram, a block scan, a scatter) and writes the tile's part of P.qsort.
+// Shade's warps mostly see one material at a time, while its path-state reads
+// stay within the tile. On the 1080p studio frame (65 materials, Disney BSDFs,
+// environment NEE): 781.2 against 770.9 Msamples/s unsorted (shade 41.5
+// against 43.3 ms, and the next extend 91.7 against 92.0); sorting the whole
+// queue gave 733.6. On the Cornell views of the batch workload (Lambertian
+// walls, quad-light NEE) shade is bound by its path-state traffic, and the
+// sorted order, which spreads a warp's path indices over the tile, doubles
+// its time at bounces 1-3 (9.3 against 5.0 ms at bounce 1 of a 1024^2 view at
+// 64 spp). Rendering therefore leaves the queue unsorted unless asked.
+// Within a tile, paths of one key land in any order; shade's results do not
+// depend on the order in which it visits paths.
+#define PYRE_SORT_TILE_N 2048  // queue entries per tile: 8 per thread of a 256-thread block
+__global__ void __launch_bounds__(256) k_sort_tile(DevScene S, PathSoA P, uint32_t depth) {
+    __shared__ uint32_t hist[PYRE_SORT_BINS];
+    __shared__ uint32_t wsum[8];
+    const uint32_t n = P.ctl->count[depth];
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const unsigned below = (1u << lane) - 1u;
+    for (uint32_t base = blockIdx.x * PYRE_SORT_TILE_N; base < n; base += gridDim.x * PYRE_SORT_TILE_N) {
+        for (uint32_t k = t; k < PYRE_SORT_BINS; k += 256) hist[k] = 0;
+        __syncthreads();
+        uint32_t key[8], rank[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const uint32_t j = base + e * 256 + t;
+            key[e] = j < n ? shade_key(S, __ldcs(P.hit_inst + j)) : PYRE_SORT_BINS;
+            const unsigned peers = __match_any_sync(0xffffffffu, key[e]);
+            const int leader = __ffs(peers) - 1;
+            uint32_t b = 0;
+            if (key[e] < PYRE_SORT_BINS && (int)lane == leader) b = atomicAdd(&hist[key[e]], (uint32_t)__popc(peers));
+            rank[e] = __shfl_sync(0xffffffffu, b, leader) + __popc(peers & below);
+        }
+        __syncthreads();
+        // exclusive scan of the bins: 4 per thread, then across the block
+        uint32_t v[PYRE_SORT_BINS / 256], sum = 0;
+#pragma unroll
+        for (int q = 0; q < PYRE_SORT_BINS / 256; ++q) { v[q] = hist[(PYRE_SORT_BINS / 256) * t + q]; sum += v[q]; }
+        uint32_t x = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        uint32_t off = x - sum;
+        for (uint32_t w = 0; w < warp; ++w) off += wsum[w];
+#pragma unroll
+        for (int q = 0; q < PYRE_SORT_BINS / 256; ++q) { hist[(PYRE_SORT_BINS / 256) * t + q] = off; off += v[q]; }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const uint32_t j = base + e * 256 + t;
+            if (j < n) P.qsort[base + hist[key[e]] + rank[e]] = j;
+        }
+        __syncthreads();
     }
 }
 
@@ -1040,8 +1118,14 @@ void launch_shadow(cudaStream_t st, const Launch& Lc, const DevScene& S, const P
 }
 
 // Orders the live paths of depth d by shade_key into P.qsort.
-void enqueue_sort(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Launch& Lc, uint32_t d) {
+// W.sort: PYRE_SORT_TILES sorts within tiles of the queue (one launch),
+// PYRE_SORT_QUEUE the whole queue (three launches).
+void enqueue_sort(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Launch& Lc, uint32_t d, int kind) {
     cudaStream_t st = ctx->stream;
+    if (kind == PYRE_SORT_TILES) {
+        k_sort_tile<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
+        return;
+    }
     k_sort_count<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
     k_sort_scan<<<1, PYRE_SORT_BINS, 0, st>>>(P);
     k_sort_scatter<<<Lc.grid_sort, 256, 0, st>>>(S, P, d);
@@ -1056,7 +1140,7 @@ void enqueue_wave(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, const Wave
         mark(ctx, STAGE_EXTEND);
         launch_extend<false>(st, Lc, S, P, W, d);
         mark(ctx, STAGE_SHADE);
-        if (W.sort) enqueue_sort(ctx, S, P, Lc, d);
+        if (W.sort) enqueue_sort(ctx, S, P, Lc, d, W.sort);
         k_shade<false><<<Lc.grid_shade, Lc.block_shade, 0, st>>>(S, P, W, d);
         if (W.ns > 0) {
             mark(ctx, STAGE_SHADOW);
@@ -1080,7 +1164,7 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
         mark(ctx, STAGE_EXTEND);
         launch_extend<true>(st, Lc, S, P, W, d);
         mark(ctx, STAGE_SHADE);
-        if (W.sort) enqueue_sort(ctx, S, P, Lc, d);
+        if (W.sort) enqueue_sort(ctx, S, P, Lc, d, W.sort);
         k_shade<true><<<Lc.grid_shade, Lc.block_shade, 0, st>>>(S, P, W, d);
         if (W.ns > 0) {
             mark(ctx, STAGE_SHADOW);
@@ -1094,7 +1178,7 @@ void enqueue_wave_batch(pyre_ctx* ctx, const DevScene& S, const PathSoA& P, cons
 }
 
 uint32_t kernels_per_wave(const WaveParams& W) {
-    return 4 + W.max_depth * ((W.ns > 0 ? 3 : 2) + (W.sort ? 3 : 0));
+    return 4 + W.max_depth * ((W.ns > 0 ? 3 : 2) + (W.sort == PYRE_SORT_TILES ? 1 : W.sort ? 3 : 0));
 }
 
 // Largest pixel count of one view: path and pixel indices are 32-bit, and a
@@ -1194,7 +1278,8 @@ static int render_impl(pyre_ctx* ctx, const pyre_scene* scene, const pyre_camera
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
     W.refill = refill_lanes(&rp);
     W.refill_any = refill_lanes(&rp, true);
-    W.sort = rp.sort_by_material == 1 ? 1 : 0;
+    W.sort = sort_kind(rp.sort_by_material, PYRE_SORT_OFF);
+    if (W.sort < 0) return set_error(ctx, PYRE_ERR_INVALID, "sort_by_material must be 0, 1, 2 or 3");
     W.prog_mean = prog;
     DevScene D;
     rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width);
@@ -1382,7 +1467,8 @@ extern "C" int pyre_render_batch(pyre_ctx* ctx, const pyre_scene* scene, const p
     W.ns = scene->part_light_max;
     W.refill = refill_lanes(params);
     W.refill_any = refill_lanes(params, true);
-    W.sort = params && params->sort_by_material == 1 ? 1 : 0;
+    W.sort = sort_kind(params ? params->sort_by_material : 0u, PYRE_SORT_OFF);
+    if (W.sort < 0) return set_error(ctx, PYRE_ERR_INVALID, "sort_by_material must be 0, 1, 2 or 3");
     DevScene D;
     int rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), params ? params->bvh_width : 0u, &D, &W.bvh_width);
     if (rc) return rc;
@@ -1561,7 +1647,8 @@ extern "C" int pyre_render_noalloc(pyre_ctx* ctx, const pyre_scene* scene, const
     W.env_cdf = rp.env_sampling == PYRE_ENV_CDF ? 1 : 0;
     W.refill = refill_lanes(&rp);
     W.refill_any = refill_lanes(&rp, true);
-    W.sort = rp.sort_by_material == 1 ? 1 : 0;
+    W.sort = sort_kind(rp.sort_by_material, PYRE_SORT_OFF);
+    if (W.sort < 0) return set_error(ctx, PYRE_ERR_INVALID, "sort_by_material must be 0, 1, 2 or 3");
     DevScene D;
     rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width, false);
     if (rc) return rc;
@@ -1824,11 +1911,12 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
     W.refill = refill_lanes(&rp);
     W.refill_any = refill_lanes(&rp, true);
     // The adjoint shade is bound by instruction fetches: warps of one
-    // material run one branch of the BSDF and gradient code. Sorting the live
-    // paths by material is the backward's default (sort_by_material 0; 2
-    // turns it off): backward 20.0 against 22.2 ms on the 512x512
-    // differentiable-render problem, the same gradients.
-    W.sort = rp.sort_by_material != 2 ? 1 : 0;
+    // material run one branch of the BSDF and gradient code. Sorting the
+    // whole live-path queue by material is the backward's default: backward
+    // 20.0 against 22.2 ms on the 512x512 differentiable-render problem, the
+    // same gradients; sorting within tiles (the render default) gave 20.5.
+    W.sort = sort_kind(rp.sort_by_material, PYRE_SORT_QUEUE);
+    if (W.sort < 0) return set_error(ctx, PYRE_ERR_INVALID, "sort_by_material must be 0, 1, 2 or 3");
     DevScene D;
     if ((rc = select_bvh(ctx, const_cast<pyre_scene*>(scene), rp.bvh_width, &D, &W.bvh_width))) return rc;
     const uint32_t spp = rp.spp_end - rp.spp_begin;
@@ -1883,7 +1971,7 @@ extern "C" int pyre_backward(pyre_ctx* ctx, const pyre_scene* scene, const pyre_
         k_raygen<false><<<Lc.grid_raygen, Lc.block_stage, 0, st>>>(S, W);
         for (uint32_t d = 0; d < W.max_depth; ++d) {
             launch_extend<false>(st, Lc, D, S, W, d);
-            if (W.sort) enqueue_sort(ctx, D, S, Lc, d);
+            if (W.sort) enqueue_sort(ctx, D, S, Lc, d, W.sort);
             k_shade<false, true><<<grid_adj, Lc.block_stage, smem, st>>>(D, S, W, d);
             if (W.ns > 0) launch_shadow<false>(st, Lc, D, S, W, d);
         }

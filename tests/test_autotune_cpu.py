@@ -69,6 +69,6 @@ def test_knob_values_are_valid_render_parameters():
     for r in AT.KNOBS["refill_lanes"]:
         assert 0 <= r <= 32
     assert set(AT.KNOBS["bvh_width"]) <= {2, 4, 8}
-    assert set(AT.KNOBS["use_graph"]) <= {0, 1} and set(AT.KNOBS["sort_by_material"]) <= {0, 1}
+    assert set(AT.KNOBS["use_graph"]) <= {0, 1} and set(AT.KNOBS["sort_by_material"]) <= {0, 1, 2, 3}
     for w in AT.KNOBS["wave_paths"]:
         assert w == 0 or w >= 1 << 20

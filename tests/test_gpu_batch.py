@@ -16,7 +16,8 @@ def _jobs():
     return P.batch_jobs(n_jobs=7, seed=5, resolutions=(32, 48, 64), spps=(1, 3, 4), tri_range=(10, 3000))
 
 
-@pytest.mark.parametrize("use_graph,sort,width", [(0, 0, 2), (1, 0, 2), (0, 1, 2), (1, 1, 4), (0, 0, 8)])
+# sort: 0 = the default (unsorted), 1 = sorted by material within tiles, 2 = unsorted, 3 = the whole queue sorted
+@pytest.mark.parametrize("use_graph,sort,width", [(0, 0, 2), (1, 2, 2), (0, 1, 2), (1, 3, 4), (0, 0, 8)])
 @pytest.mark.parametrize("wave_paths", [0, 9000])
 def test_batch_matches_single_renders(gpu_ctx, use_graph, sort, width, wave_paths):
     jobs = _jobs()

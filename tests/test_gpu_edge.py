@@ -143,3 +143,18 @@ def test_crop_area_above_2_31_is_rejected_before_any_work(gpu_ctx):
     assert np.isfinite(film.radiance).all()
     db.close()
     ds.close()
+
+
+def test_unknown_sort_kind_is_rejected(gpu_ctx):
+    """sort_by_material takes 0 (the call's default), 1 (within tiles), 2 (off) and 3 (the whole queue)."""
+    from pyre_gb300 import native as N
+    from pyre_gb300.scene import Film
+    sc, cam = P.cornell_ref(), P.cornell_ref_camera(32, 16)
+    ds = gpu_ctx.upload(sc)
+    film = Film(32, 16)
+    f = N.Film(N.fptr(film.radiance), N.fptr(film.albedo), N.fptr(film.normal), N.fptr(film.depth), N.PYRE_MEM_HOST)
+    p = gpu_ctx.params(32, 16, 0, 1, PathIntegrator(8, 3))
+    p.sort_by_material = 4
+    with pytest.raises(PyreError, match="sort_by_material"):
+        gpu_ctx.render_into(ds, cam, p, f)
+    ds.close()

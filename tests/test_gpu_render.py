@@ -113,8 +113,9 @@ def test_procedural_studio_small(gpu_ctx, oracle_mod):
     _check(film, ref, bar=1e-2)
 
 
-@pytest.mark.parametrize("refill,sort,width", [(1, 0, 2), (4, 0, 2), (32, 0, 2), (8, 1, 2), (32, 1, 2), (16, 0, 4),
-                                               (16, 0, 8), (4, 1, 4), (32, 1, 8)])
+# sort: 2 = unsorted, 1 = sorted by material within tiles, 3 = the whole queue sorted
+@pytest.mark.parametrize("refill,sort,width", [(1, 2, 2), (4, 2, 2), (32, 2, 2), (8, 1, 2), (32, 3, 2), (16, 2, 4),
+                                               (16, 2, 8), (4, 1, 4), (32, 3, 8)])
 def test_traversal_and_shade_order_do_not_change_results(gpu_ctx, refill, sort, width):
     """The traversal kernels refetch rays into finished lanes, can walk 4- or
     8-wide instance BVHs, and shade can visit the live paths sorted by
