@@ -139,6 +139,19 @@ __device__ __forceinline__ void ldg_256(const float4* p, float4& a, float4& b) {
         : "l"(p));
 }
 
+// 32-B path-state records with one streaming (evict-first) 256-bit load or
+// store each; p must be 32-B aligned.
+__device__ __forceinline__ void ldcs_256(const float4* p, float4& a, float4& b) {
+    asm("ld.global.cs.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+__device__ __forceinline__ void stcs_256(float4* p, const float4& a, const float4& b) {
+    asm volatile("st.global.cs.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                 :: "l"(p), "f"(a.x), "f"(a.y), "f"(a.z), "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+                 : "memory");
+}
+
 // Rust-order slab test (bvh.rs:146-153): t1/t2 per axis, max of mins vs
 // t_min, min of maxes vs t_max, hit iff tmin <= tmax. Returns the entry.
 __device__ __forceinline__ bool slab(float lox, float hix, float loy, float hiy, float loz, float hiz,

@@ -152,8 +152,8 @@ struct PathSoA {
     float4* hit;       // t, u, v, triangle slot (bits)
     int32_t* hit_inst; // instance slot; -1 miss; -2-l quad light l
     uint4* rng;        // 2 per path
-    float4* beta;      // throughput.xyz, pdf of the last BSDF sample
-    float4* L;         // radiance.xyz
+    float4* Lb;        // 2 per path, one 32-B record: radiance.xyz, -; throughput.xyz, pdf of the
+                       // last BSDF sample (shade reads and writes both with one access each)
     float4* aov_a;     // albedo.xyz, depth
     float4* aov_n;     // normal.xyz
     float4* pend;      // ns per path: NEE contribution.xyz, w = 1 while pending
@@ -181,19 +181,22 @@ __device__ __forceinline__ uint32_t append_slot(uint32_t* counter) {
     return base + g.thread_rank();
 }
 
+// A path's generator state is one 32-B record: one 256-bit access each way.
 __device__ __forceinline__ void store_rng(uint4* r, uint32_t i, const Rng& g) {
-    __stcs(r + 2 * (size_t)i,
-           make_uint4((uint32_t)g.s0, (uint32_t)(g.s0 >> 32), (uint32_t)g.s1, (uint32_t)(g.s1 >> 32)));
-    __stcs(r + 2 * (size_t)i + 1,
-           make_uint4((uint32_t)g.s2, (uint32_t)(g.s2 >> 32), (uint32_t)g.s3, (uint32_t)(g.s3 >> 32)));
+    auto f = [](uint64_t v, int hi) { return __uint_as_float((uint32_t)(hi ? v >> 32 : v)); };
+    stcs_256(reinterpret_cast<float4*>(r + 2 * (size_t)i),
+             make_float4(f(g.s0, 0), f(g.s0, 1), f(g.s1, 0), f(g.s1, 1)),
+             make_float4(f(g.s2, 0), f(g.s2, 1), f(g.s3, 0), f(g.s3, 1)));
 }
 __device__ __forceinline__ Rng load_rng(const uint4* r, uint32_t i) {
-    const uint4 a = __ldcs(r + 2 * (size_t)i), b = __ldcs(r + 2 * (size_t)i + 1);
+    float4 a, b;
+    ldcs_256(reinterpret_cast<const float4*>(r + 2 * (size_t)i), a, b);
+    auto u = [](float lo, float hi) { return (uint64_t)__float_as_uint(lo) | ((uint64_t)__float_as_uint(hi) << 32); };
     Rng g;
-    g.s0 = (uint64_t)a.x | ((uint64_t)a.y << 32);
-    g.s1 = (uint64_t)a.z | ((uint64_t)a.w << 32);
-    g.s2 = (uint64_t)b.x | ((uint64_t)b.y << 32);
-    g.s3 = (uint64_t)b.z | ((uint64_t)b.w << 32);
+    g.s0 = u(a.x, a.y);
+    g.s1 = u(a.z, a.w);
+    g.s2 = u(b.x, b.y);
+    g.s3 = u(b.z, b.w);
     return g;
 }
 
@@ -285,7 +288,7 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
         // radiance 0, throughput 1 and the AOVs are set by shade at depth 0;
         // with max_depth 0 no vertex is shaded and the sample is all zeros
         if (max_depth == 0) {
-            P.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            P.Lb[2 * (size_t)i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             __stcs(&P.aov_a[i], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
             __stcs(&P.aov_n[i], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         }
@@ -587,7 +590,8 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
         // a batch wave traces every job's camera rays; a job with max_depth 0 shades none
         if (BATCH && depth == 0 && JB->max_depth == 0) continue;
         // a camera path starts with radiance 0 and throughput 1 (integrator.rs:63-64)
-        const float4 Lq = depth > 0 ? __ldcs(P.L + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float4 Lq = make_float4(0.0f, 0.0f, 0.0f, 0.0f), bq = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        if (depth > 0) ldcs_256(P.Lb + 2 * (size_t)i, Lq, bq);
         f3 L = mk3(Lq.x, Lq.y, Lq.z);
         f3 delta = splat3(0.0f), Ltot = splat3(0.0f);
         if (ADJ) {  // adjoint of this path's film pixel, and its forward radiance
@@ -627,9 +631,9 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
             }
         }
         if (ADJ) warp_flush(S, W.env_grad, W.mat_grad, G, gt);
-        const float4 bq = depth > 0 ? __ldcs(P.beta + i) : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         f3 beta = mk3(bq.x, bq.y, bq.z);
         const float last_pdf = bq.w;
+        float next_pdf = last_pdf;  // stored with the throughput: the pdf of this vertex's BSDF sample
         const float4 ro = BATCH ? ro_b : __ldcs(P.ray_o[depth & 1] + pos), rd = __ldcs(P.ray_d[depth & 1] + pos);
         const f3 ray_o = mk3(ro.x, ro.y, ro.z), ray_d = mk3(rd.x, rd.y, rd.z);
         const float time = rd.w;
@@ -771,7 +775,7 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
                                        make_float4(p_off.x, p_off.y, p_off.z, BATCH ? ro.w : 1e-4f));
                                 __stcs(P.ray_d[(depth + 1) & 1] + q, make_float4(nd.x, nd.y, nd.z, time));
                             }
-                            __stcs(P.beta + i, make_float4(beta.x, beta.y, beta.z, pdf_b));
+                            next_pdf = pdf_b;
                             if (ADJ) {  // for the next vertex's BSDF-sample gradient
                                 P.brec[3 * (size_t)i] = make_float4(wo.x, wo.y, wo.z, __uint_as_float(I.material));
                                 P.brec[3 * (size_t)i + 1] = make_float4(wi.x, wi.y, wi.z, 1.0f);
@@ -816,7 +820,8 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
                 store_rng(P.rng, i, g);
             }
         }
-        __stcs(P.L + i, make_float4(L.x, L.y, L.z, 0.0f));
+        // a path without a next ray is not read again, whatever its throughput
+        stcs_256(P.Lb + 2 * (size_t)i, make_float4(L.x, L.y, L.z, 0.0f), make_float4(beta.x, beta.y, beta.z, next_pdf));
     }
     if (ADJ) grad_smem_end(G, W.env_grad, W.mat_grad, W.n_mat);  // one atomic per parameter / texel per block
 }
@@ -847,7 +852,7 @@ __global__ void k_accumulate(PathSoA P, WaveParams W) {
             mean = mk3(W.prog_mean[3 * (size_t)p], W.prog_mean[3 * (size_t)p + 1], W.prog_mean[3 * (size_t)p + 2]);
         for (uint32_t k = 0; k < kv; ++k) {
             uint32_t i = k * W.npix + p;
-            const float4 Lq = __ldcs(P.L + i);  // last reads of the path state
+            const float4 Lq = __ldcs(P.Lb + 2 * (size_t)i);  // last reads of the path state
             f3 L = mk3(Lq.x, Lq.y, Lq.z);
             for (uint32_t s = 0; s < W.ns; ++s) {
                 const float4 c = __ldcs(P.pend + (size_t)i * W.ns + s);
@@ -886,7 +891,7 @@ __global__ void k_accumulate_batch(PathSoA P, WaveParams W) {
         float4 ar = P.acc_r[a], aa = P.acc_a[a], an = P.acc_n[a];
         for (uint32_t k = 0; k < sg.s_count; ++k) {
             const uint32_t i = sg.path_base + k * J.npix + p;
-            const float4 Lq = __ldcs(P.L + i);  // last reads of the path state
+            const float4 Lq = __ldcs(P.Lb + 2 * (size_t)i);  // last reads of the path state
             f3 L = mk3(Lq.x, Lq.y, Lq.z);
             for (uint32_t s = 0; s < W.ns; ++s) {
                 const float4 c = __ldcs(P.pend + (size_t)i * W.ns + s);
@@ -1011,8 +1016,7 @@ size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* ou
     s.hit = c.take<float4>(P);
     s.hit_inst = c.take<int32_t>(P);
     s.rng = c.take<uint4>(2 * P);
-    s.beta = c.take<float4>(P);
-    s.L = c.take<float4>(P);
+    s.Lb = c.take<float4>(2 * P);
     s.aov_a = c.take<float4>(P);
     s.aov_n = c.take<float4>(P);
     s.pend = c.take<float4>(P * ns);
