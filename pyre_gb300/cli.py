@@ -52,6 +52,9 @@ def parse(argv=None):
     ap.add_argument("--query", default="closest", choices=["closest", "any", "both"])
     ap.add_argument("--level", type=int, default=8, help="microbench: icosphere subdivision level")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 4, 8], help="instance BVH width")
+    ap.add_argument("--sort", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="shade queue order (sort_by_material): 0 = the library default, 1 = sorted by material "
+                         "within tiles, 2 = unsorted, 3 = the whole queue sorted")
     return ap.parse_args(argv)
 
 
@@ -223,7 +226,7 @@ def main(argv=None) -> int:
     for _ in range(args.repeat):
         t0 = time.perf_counter()
         film = ctx.render(ds, cam, integ, args.width, args.height, args.spp, env_sampling=env,
-                          use_graph=1 if args.graph else 0)
+                          use_graph=1 if args.graph else 0, sort_by_material=args.sort)
         dt = time.perf_counter() - t0
         s = ctx.stats()
         print(json.dumps({"preset": args.preset, "elapsed_ms": dt * 1e3, "device_ms": s.ms_total,

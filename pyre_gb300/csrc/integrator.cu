@@ -154,8 +154,7 @@ struct PathSoA {
     uint4* rng;        // 2 per path
     float4* Lb;        // 2 per path, one 32-B record: radiance.xyz, -; throughput.xyz, pdf of the
                        // last BSDF sample (shade reads and writes both with one access each)
-    float4* aov_a;     // albedo.xyz, depth
-    float4* aov_n;     // normal.xyz
+    float4* aov;       // 2 per path, one 32-B record: albedo.xyz, depth; normal.xyz, -
     float4* pend;      // ns per path: NEE contribution.xyz, w = 1 while pending
     float4* sh_o;      // per shadow-queue entry: shadow origin.xyz, t_max
     float4* sh_d;      // per shadow-queue entry: shadow direction.xyz, time
@@ -289,8 +288,7 @@ __global__ void k_raygen(PathSoA P, WaveParams W) {
         // with max_depth 0 no vertex is shaded and the sample is all zeros
         if (max_depth == 0) {
             P.Lb[2 * (size_t)i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            __stcs(&P.aov_a[i], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
-            __stcs(&P.aov_n[i], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+            stcs_256(P.aov + 2 * (size_t)i, make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         }
         for (uint32_t s = 0; s < W.ns; ++s) __stcs(P.pend + (size_t)i * W.ns + s, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     }
@@ -642,8 +640,8 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
 
         if (code == -1) {
             if (depth == 0) {  // a camera ray that escapes leaves the AOVs at zero
-                __stcs(&P.aov_a[i], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
-                __stcs(&P.aov_n[i], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+                stcs_256(P.aov + 2 * (size_t)i, make_float4(0.0f, 0.0f, 0.0f, 0.0f),
+                         make_float4(0.0f, 0.0f, 0.0f, 0.0f));
             }
             // Escaped: environment radiance with MIS against the BSDF arm (integrator.rs:243-259).
             if (S.has_env) {
@@ -666,8 +664,8 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
             // Quad light hit (integrator.rs:262-295).
             const DevQuadLight& Lt = S.lights[-2 - code];
             if (depth == 0) {
-                __stcs(&P.aov_a[i], make_float4(1.0f, 1.0f, 1.0f, hq.x));
-                __stcs(&P.aov_n[i], make_float4(Lt.normal.x, Lt.normal.y, Lt.normal.z, 0.0f));
+                stcs_256(P.aov + 2 * (size_t)i, make_float4(1.0f, 1.0f, 1.0f, hq.x),
+                         make_float4(Lt.normal.x, Lt.normal.y, Lt.normal.z, 0.0f));
             }
             f3 le = dot3(Lt.normal, -ray_d) > 0.0f ? Lt.emission : splat3(0.0f);
             if (last_was_specular) L = L + beta * le;
@@ -701,8 +699,8 @@ __global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene
             }
             const Bsdf mat = load_bsdf(S, I.material);
             if (depth == 0) {
-                __stcs(&P.aov_a[i], make_float4(mat.base.x, mat.base.y, mat.base.z, t));
-                __stcs(&P.aov_n[i], make_float4(ns.x, ns.y, ns.z, 0.0f));
+                stcs_256(P.aov + 2 * (size_t)i, make_float4(mat.base.x, mat.base.y, mat.base.z, t),
+                         make_float4(ns.x, ns.y, ns.z, 0.0f));
             }
             const Frame3 fr = frame_from_normal(ns);
             const f3 wo = to_local(fr, -ray_d);
@@ -863,7 +861,8 @@ __global__ void k_accumulate(PathSoA P, WaveParams W) {
                 const float n = (float)(P.ctl->s_base + k + 1);
                 mean = mean + (L - mean) / n;
             }
-            const float4 a = __ldcs(P.aov_a + i), nn = __ldcs(P.aov_n + i);
+            float4 a, nn;
+            ldcs_256(P.aov + 2 * (size_t)i, a, nn);
             ar.x += L.x; ar.y += L.y; ar.z += L.z; ar.w += a.w;
             aa.x += a.x; aa.y += a.y; aa.z += a.z;
             an.x += nn.x; an.y += nn.y; an.z += nn.z;
@@ -897,7 +896,8 @@ __global__ void k_accumulate_batch(PathSoA P, WaveParams W) {
                 const float4 c = __ldcs(P.pend + (size_t)i * W.ns + s);
                 if (c.w != 0.0f) L = L + mk3(c.x, c.y, c.z);
             }
-            const float4 al = __ldcs(P.aov_a + i), nn = __ldcs(P.aov_n + i);
+            float4 al, nn;
+            ldcs_256(P.aov + 2 * (size_t)i, al, nn);
             ar.x += L.x; ar.y += L.y; ar.z += L.z; ar.w += al.w;
             aa.x += al.x; aa.y += al.y; aa.z += al.z;
             an.x += nn.x; an.y += nn.y; an.z += nn.z;
@@ -1017,8 +1017,7 @@ size_t carve_paths(char* base, size_t P, uint32_t ns, uint32_t npix, PathSoA* ou
     s.hit_inst = c.take<int32_t>(P);
     s.rng = c.take<uint4>(2 * P);
     s.Lb = c.take<float4>(2 * P);
-    s.aov_a = c.take<float4>(P);
-    s.aov_n = c.take<float4>(P);
+    s.aov = c.take<float4>(2 * P);
     s.pend = c.take<float4>(P * ns);
     s.sh_o = c.take<float4>(P * ns);
     s.sh_d = c.take<float4>(P * ns);

@@ -370,26 +370,27 @@ class CudaIntegrator:
 
     @staticmethod
     def params(width, height, spp_begin, spp_end, integrator: PathIntegrator, crop=None, env_sampling=0,
-               wave_paths=0, use_graph=0, block_size=0, refill_lanes=0, bvh_width=0) -> N.RenderParams:
+               wave_paths=0, use_graph=0, block_size=0, refill_lanes=0, bvh_width=0,
+               sort_by_material=0) -> N.RenderParams:
         p = N.RenderParams()
         p.width, p.height, p.spp_begin, p.spp_end = width, height, spp_begin, spp_end
         p.max_depth, p.min_rr_depth = integrator.max_depth, integrator.min_rr_depth
         if crop is not None:
             p.crop[:] = list(crop)
         p.env_sampling, p.wave_paths, p.use_graph, p.block_size = env_sampling, wave_paths, use_graph, block_size
-        p.refill_lanes, p.bvh_width = refill_lanes, bvh_width
+        p.refill_lanes, p.bvh_width, p.sort_by_material = refill_lanes, bvh_width, sort_by_material
         return p
 
     def render(self, dscene: DeviceScene, camera: CameraSpec, integrator: PathIntegrator, width: int, height: int,
                spp: int, spp_begin: int = 0, crop=None, env_sampling: int = 0, wave_paths: int = 0,
-               use_graph: int = 0, refill_lanes: int = 0, bvh_width: int = 0) -> Film:
+               use_graph: int = 0, refill_lanes: int = 0, bvh_width: int = 0, sort_by_material: int = 0) -> Film:
         """Renders samples [spp_begin, spp_begin+spp) into a (crop-sized) host Film."""
         x0, y0, x1, y1 = crop if crop is not None else (0, 0, width, height)
         film = Film(x1 - x0, y1 - y0)
         f = N.Film(N.fptr(film.radiance), N.fptr(film.albedo), N.fptr(film.normal), N.fptr(film.depth), N.PYRE_MEM_HOST)
         cam = camera.to_desc()
         p = self.params(width, height, spp_begin, spp_begin + spp, integrator, crop, env_sampling, wave_paths, use_graph,
-                        refill_lanes=refill_lanes, bvh_width=bvh_width)
+                        refill_lanes=refill_lanes, bvh_width=bvh_width, sort_by_material=sort_by_material)
         self.check(self.lib.pyre_render(self.handle, dscene.handle, C.byref(cam), C.byref(p), C.byref(f)))
         return film
 
