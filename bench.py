@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--graph", type=int, default=0, help="replay waves through a CUDA graph")
     ap.add_argument("--bvh-width", type=int, default=0, help="instance BVH width 2, 4 or 8 (0 = 2)")
     ap.add_argument("--sort", type=int, default=1,
-                    help="shade queue order (sort_by_material): 1 = sorted by material within tiles of 2048 "
+                    help="shade queue order (sort_by_material): 1 = sorted by material within tiles of 4096 "
                          "entries (the fastest on this frame), 0 = the library default (unsorted), 2 = unsorted, "
                          "3 = the whole queue sorted")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths in flight per wave (0 = library default)")

@@ -267,7 +267,7 @@ typedef struct pyre_render_params {
                                         for the forward shade, 128 for the traversals);
                                         0 = 256 / 224 / 128 */
     uint32_t sort_by_material;       /* order the shade queue by material: 1 = within
-                                        tiles of 2048 entries, 2 = off, 3 = the whole
+                                        tiles of 4096 entries, 2 = off, 3 = the whole
                                         queue, 0 = the default (off; 3 in pyre_backward) */
     uint32_t use_graph;              /* capture one wave as a CUDA graph and replay it */
     uint32_t refill_lanes;           /* traversal: refetch rays once this many lanes of a

@@ -36,6 +36,13 @@ namespace pyre {
 // (with instances entered from the top-level step, 9 closest-hit blocks
 // measured 746.2 against 737.9 Msamples/s for 10 and 743.4 for 8; any hit at
 // 10 blocks took 36.0 against 34.5 ms of shadow)
+// forward shade: threads per block and resident blocks per SM
+#ifndef PYRE_SHADE_THREADS
+#define PYRE_SHADE_THREADS 224
+#endif
+#ifndef PYRE_SHADE_BLOCKS
+#define PYRE_SHADE_BLOCKS 4
+#endif
 #ifndef PYRE_TRACE_BLOCKS
 #define PYRE_TRACE_BLOCKS 9
 #endif
@@ -500,16 +507,22 @@ __global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
 // histogram, a block scan, a scatter) and writes the tile's part of P.qsort.
 // Shade's warps mostly see one material at a time, while its path-state reads
 // stay within the tile. On the 1080p studio frame (65 materials, Disney BSDFs,
-// environment NEE): 781.2 against 770.9 Msamples/s unsorted (shade 41.5
-// against 43.3 ms, and the next extend 91.7 against 92.0); sorting the whole
-// queue gave 733.6. On the Cornell views of the batch workload (Lambertian
+// environment NEE), with tiles of 2048 entries: 781.2 against 770.9
+// Msamples/s unsorted (shade 41.5 against 43.3 ms, and the next extend 91.7
+// against 92.0); sorting the whole queue gave 733.6. On the Cornell views of the batch workload (Lambertian
 // walls, quad-light NEE) shade is bound by its path-state traffic, and the
 // sorted order, which spreads a warp's path indices over the tile, doubles
 // its time at bounces 1-3 (9.3 against 5.0 ms at bounce 1 of a 1024^2 view at
 // 64 spp). Rendering therefore leaves the queue unsorted unless asked.
 // Within a tile, paths of one key land in any order; shade's results do not
 // depend on the order in which it visits paths.
-#define PYRE_SORT_TILE_N 2048  // queue entries per tile: 8 per thread of a 256-thread block
+// Queue entries per tile, PYRE_SORT_TILE_E per thread of a 256-thread block:
+// on the 1080p studio frame 1024 / 2048 / 4096 / 8192 / 16384 entries gave
+// 766.5 / 784.2 / 793.4 / 791.0 / 782.4 Msamples/s.
+#ifndef PYRE_SORT_TILE_N
+#define PYRE_SORT_TILE_N 4096
+#endif
+#define PYRE_SORT_TILE_E (PYRE_SORT_TILE_N / 256)
 __global__ void __launch_bounds__(256) k_sort_tile(DevScene S, PathSoA P, uint32_t depth) {
     __shared__ uint32_t hist[PYRE_SORT_BINS];
     __shared__ uint32_t wsum[8];
@@ -519,9 +532,9 @@ __global__ void __launch_bounds__(256) k_sort_tile(DevScene S, PathSoA P, uint32
     for (uint32_t base = blockIdx.x * PYRE_SORT_TILE_N; base < n; base += gridDim.x * PYRE_SORT_TILE_N) {
         for (uint32_t k = t; k < PYRE_SORT_BINS; k += 256) hist[k] = 0;
         __syncthreads();
-        uint32_t key[8], rank[8];
+        uint32_t key[PYRE_SORT_TILE_E], rank[PYRE_SORT_TILE_E];
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
+        for (int e = 0; e < PYRE_SORT_TILE_E; ++e) {
             const uint32_t j = base + e * 256 + t;
             key[e] = j < n ? shade_key(S, __ldcs(P.hit_inst + j)) : PYRE_SORT_BINS;
             const unsigned peers = __match_any_sync(0xffffffffu, key[e]);
@@ -549,7 +562,7 @@ __global__ void __launch_bounds__(256) k_sort_tile(DevScene S, PathSoA P, uint32
         for (int q = 0; q < PYRE_SORT_BINS / 256; ++q) { hist[(PYRE_SORT_BINS / 256) * t + q] = off; off += v[q]; }
         __syncthreads();
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
+        for (int e = 0; e < PYRE_SORT_TILE_E; ++e) {
             const uint32_t j = base + e * 256 + t;
             if (j < n) P.qsort[base + hist[key[e]] + rank[e]] = j;
         }
@@ -566,7 +579,7 @@ __global__ void __launch_bounds__(256) k_sort_tile(DevScene S, PathSoA P, uint32
 // registers) by 0.3 % on the 1080p studio frame. The adjoint variant keeps
 // 3 blocks of 256: at 72 registers its spills would grow.
 template <bool BATCH, bool ADJ = false>
-__global__ void __launch_bounds__(ADJ ? 256 : 224, ADJ ? 3 : 4) k_shade(DevScene S, PathSoA P, WaveParams W,
+__global__ void __launch_bounds__(ADJ ? 256 : PYRE_SHADE_THREADS, ADJ ? 3 : PYRE_SHADE_BLOCKS) k_shade(DevScene S, PathSoA P, WaveParams W,
                                                                         uint32_t depth) {
     GradSmem G{nullptr, nullptr, nullptr};
     if (ADJ) G = grad_smem_begin(W.env_cache != 0, W.smem_grad != 0, W.n_mat);
@@ -1057,7 +1070,7 @@ uint64_t default_wave_paths(pyre_ctx* ctx, uint32_t ns, bool batch, bool adjoint
 
 struct Launch {
     int block_stage = 256;  // raygen, accumulate, adjoint shade (at most 256)
-    int block_shade = 224;  // forward shade (at most 224)
+    int block_shade = PYRE_SHADE_THREADS;  // forward shade (at most PYRE_SHADE_THREADS)
     int block_trace = 128;  // extend, shadow (at most 128)
     int grid_raygen, grid_shade, grid_extend, grid_shadow, grid_acc, grid_sort;
 };
@@ -1072,7 +1085,7 @@ Launch make_launch(pyre_ctx* ctx, uint32_t block_size, int width) {
     if (block_size) {
         const int b = (int)std::max(32u, std::min(256u, block_size / 32 * 32));
         L.block_stage = b;
-        L.block_shade = std::min(b, 224);
+        L.block_shade = std::min(b, PYRE_SHADE_THREADS);
         L.block_trace = std::min(b, 128);
     }
     L.grid_raygen = grid_for(ctx, k_raygen<BATCH>, L.block_stage);
