@@ -525,6 +525,8 @@ __global__ void k_sort_scatter(DevScene S, PathSoA P, uint32_t depth) {
 #define PYRE_SORT_TILE_N 4096
 #endif
 #define PYRE_SORT_TILE_E (PYRE_SORT_TILE_N / 256)
+static_assert(PYRE_SORT_TILE_N % 256 == 0 && PYRE_SORT_TILE_N >= 256, "a tile is whole 256-thread rows");
+static_assert(PYRE_SORT_BINS % 256 == 0, "k_sort_tile scans PYRE_SORT_BINS / 256 bins per thread");
 __global__ void __launch_bounds__(256) k_sort_tile(DevScene S, PathSoA P, uint32_t depth) {
     __shared__ uint32_t hist[PYRE_SORT_BINS];
     __shared__ uint32_t wsum[8];
