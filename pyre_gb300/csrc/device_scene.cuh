@@ -225,7 +225,8 @@ __device__ __forceinline__ f3 motion_offset(const DevInstance& I, float time) {
 // lock step. An any-hit lane that finds a hit is finished at the end of that
 // leaf phase.
 //
-// Src supplies the rays and takes the results:
+// Src supplies the rays and takes the results (and kTmin / kTmax, the t range
+// that idle lanes start with: the range of every ray where it is fixed):
 //   uint32_t load(uint32_t j, TraceRay& r, int32_t& root)  ray j of the queue,
 //            the top-level root to trace; returns the id passed to store
 //   void store(uint32_t id, const TraceRay& r, TraceHit& h, bool found)
@@ -286,7 +287,8 @@ __device__ __forceinline__ void trace_stream(const DevScene& S, const Src& src, 
     bool active = false;    // the lane holds a ray
     uint32_t id = 0;
     TraceRay r;
-    r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.tmin = 0.0f; r.tmax = 0.0f; r.time = 0.0f; r.job = 0;
+    r.o = splat3(0.0f); r.d = mk3(0.0f, 0.0f, 1.0f); r.time = 0.0f; r.job = 0;
+    r.tmin = Src::kTmin; r.tmax = Src::kTmax;  // a source whose rays share one range makes it a constant
     TraceHit hit;
     hit.inst = -1; hit.tri = -1; hit.light = -1; hit.t = 0.0f; hit.u = 0.0f; hit.v = 0.0f;
     f3 inv = splat3(0.0f);
